@@ -1,0 +1,169 @@
+/*
+ * topopt_gb300.h -- C ABI of libtopopt_gb300.so, a GB300 (sm_103a) drop-in for
+ * the per-design-iteration SIMP compliance loop of TopOpt.jl.
+ *
+ * All functions return an int status (TOG_OK = 0).  On failure the message is
+ * available from tog_last_error() (thread-local).  Arrays are plain host
+ * pointers unless a name ends in _dev; indices are 0-based (TopOpt.jl is
+ * 1-based: a dof d there is d-1 here).  Dof-sized vectors are in the
+ * reference's Ferrite dof order; element-sized vectors in the reference's cell
+ * order (x fastest).  A handle owns its device memory and one CUDA stream; it
+ * is not thread-safe (one handle per Julia task), as the reference solver.
+ *
+ * Each entry point names the TopOpt.jl interface it replaces (paths relative
+ * to the TopOpt.jl project root).
+ */
+#ifndef TOPOPT_GB300_H
+#define TOPOPT_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TOG_ABI_VERSION 1
+
+enum tog_status {
+    TOG_OK = 0,
+    TOG_ERR_ARG = 1,           /* ArgumentError / DimensionMismatch in the reference */
+    TOG_ERR_CUDA = 2,          /* CUDA runtime error (message in tog_last_error) */
+    TOG_NOT_CONVERGED = 3,     /* PCG stopped at maxiter (the reference's cg! returns silently) */
+    TOG_BREAKDOWN = 4,         /* p'Kp <= 0 or NaN: operator not positive definite */
+    TOG_ERR_STATE = 5,         /* call order violated (e.g. compliance before a solve) */
+    TOG_ERR_OOM = 6            /* device allocation failed */
+};
+
+enum tog_precision {
+    TOG_FP64 = 0,              /* plain FP64 Jacobi PCG */
+    TOG_FP32_IR = 1            /* FP32 K*u and PCG inside FP64 iterative refinement */
+};
+
+enum tog_filter_kind { TOG_FILTER_NONE = 0, TOG_FILTER_DENSITY = 1, TOG_FILTER_SENS = 2 };
+enum tog_filter_op { TOG_FILTER_J = 0, TOG_FILTER_JT = 1 };
+
+typedef struct tog_handle tog_handle;
+
+/* Problem and solver settings: PointLoadCantilever / HalfMBB grid
+ * (src/TopOptProblems/problem_types.jl:162-231, 324-395), material
+ * (matrices_and_vectors.jl:83-84) and FEASolver keywords xmin / penalty
+ * (src/FEA/solvers_api.jl:468-489). */
+typedef struct tog_problem_desc {
+    int32_t dim;            /* 2 (quad4) or 3 (hex8) */
+    int32_t nel[3];         /* elements per axis (nel[2] ignored in 2D) */
+    double size[3];         /* element edge lengths */
+    double E;               /* Young's modulus E0 */
+    double nu;              /* Poisson ratio */
+    int32_t plane_stress;   /* 0 = plane strain, as the reference; 1 = plane stress (2D extra) */
+    double xmin;            /* rho = xmin + (1 - xmin) x^p */
+    double penalty;         /* PowerPenaltyFun exponent p */
+} tog_problem_desc;
+
+typedef struct tog_solve_stats {
+    int32_t status;          /* TOG_OK, TOG_NOT_CONVERGED or TOG_BREAKDOWN */
+    int32_t iterations;      /* PCG iterations (sum of inner iterations for FP32-IR) */
+    int32_t outer_iterations;/* refinement steps (0 for FP64) */
+    int32_t reserved;
+    double rel_residual;     /* ||f - K u|| / ||f|| (FP64 true residual for FP32-IR) */
+    double abs_residual;
+} tog_solve_stats;
+
+typedef struct tog_iter_stats {
+    double compliance;       /* c = sum rho_e u_e' Ke u_e at the filtered design */
+    double volume;           /* volume fraction of the filtered design before the OC step */
+    double change;           /* max |x_new - x| */
+    double lambda;           /* OC multiplier */
+    int32_t cg_iterations;
+    int32_t outer_iterations;
+    int32_t oc_steps;
+    int32_t status;
+    double rel_residual;
+} tog_iter_stats;
+
+/* ---- library -------------------------------------------------------------------- */
+const char* tog_version(void);
+const char* tog_last_error(void);
+/* Number of kernels this process launched through the library (graph nodes included). */
+int64_t tog_launch_count(void);
+
+/* ---- host-only helpers (no GPU needed) ------------------------------------------ */
+/* Grid sizes of RectilinearGrid (src/TopOptProblems/grids.jl:66-92). */
+int tog_grid_counts(int32_t dim, const int32_t* nel, int64_t* nnodes, int64_t* ncells, int64_t* ndofs);
+/* Metadata.node_dofs (src/TopOptProblems/metadata.jl:116-145): node_dofs[n*dim+c],
+ * node n in the reference's node order (x fastest); 0-based dofs. */
+int tog_node_dofs(int32_t dim, const int32_t* nel, int32_t* node_dofs);
+/* Metadata.cell_dofs (metadata.jl:40-50): cell_dofs[e*ndpc + dim*a + c]. */
+int tog_cell_dofs(int32_t dim, const int32_t* nel, int32_t* cell_dofs);
+/* One element stiffness matrix Ke (matrices_and_vectors.jl:68-177), Ferrite dof order,
+ * row-major ndpc x ndpc. */
+int tog_element_stiffness(int32_t dim, const double* size, double E, double nu, int32_t plane_stress,
+                          double* Ke);
+
+/* ---- solver handle: FEASolver(GB300Solver, problem; xmin, penalty)
+ *      (replaces FEASolver(CGMatrixFreeSolver, ...), src/FEA/solvers_api.jl:468-593) -- */
+int tog_create(const tog_problem_desc* desc, tog_handle** out);
+int tog_destroy(tog_handle* h);
+/* Launch on the caller's stream (cudaStream_t as void*); NULL restores the handle's own. */
+int tog_set_stream(tog_handle* h, void* stream);
+/* problem.ch.prescribed_dofs (homogeneous Dirichlet; solvers_api.jl:515-530). */
+int tog_set_fixed_dofs(tog_handle* h, int64_t n, const int32_t* dofs);
+/* globalinfo.f, dense, reference dof order (matrices_and_vectors.jl:346-365). */
+int tog_set_rhs(tog_handle* h, const double* f);
+/* setpenalty!(solver, p) (solvers_api.jl:417-427). */
+int tog_set_penalty(tog_handle* h, double p);
+/* solver.vars .= x  (compliance.jl:65): the filtered pseudo-densities, one per cell. */
+int tog_set_vars(tog_handle* h, const double* x);
+/* mul!(y, ::MatrixFreeOperator, x) (matrix_free_operator.jl:66-105), FP64, reference order. */
+int tog_matvec(tog_handle* h, const double* x, double* y);
+/* solver() -> solve_system!(CGMatrixFreeSolver, ...) (solvers_api.jl:253-282, 177-220):
+ * Jacobi PCG to ||f - K u|| <= max(rtol*||f||, abstol).  warm_start != 0 starts from the
+ * current u (previous solve or tog_set_u) instead of 0. */
+int tog_solve(tog_handle* h, int32_t precision, double rtol, double abstol, int32_t maxiter, int32_t warm_start,
+              tog_solve_stats* stats);
+/* solver.u (reference dof order). */
+int tog_get_u(tog_handle* h, double* u);
+int tog_set_u(tog_handle* h, const double* u);
+/* ComplianceFun call + rrule (compliance.jl:58-76, compute_element_energy.jl:18-38):
+ * c = sum rho_e u_e'Ke u_e at the current vars and u; grad (may be NULL) = dc/dvars. */
+int tog_compliance(tog_handle* h, double* c, double* grad);
+
+/* ---- filters: DensityFilterFun / SensFilterFun (src/CheqFilters/density_filter.jl:25-121,
+ *      sens_filter.jl:29-111, CheqFilters.jl:66-118) ---------------------------------- */
+/* Build the node-based filter of radius rmin (TOG_ERR_ARG if no cell has a node within rmin,
+ * as DensityFilterFun's ArgumentError). */
+int tog_filter_setup(tog_handle* h, double rmin);
+/* op = TOG_FILTER_J: y = J x (DensityFilterFun forward, SensFilterFun pullback);
+ * op = TOG_FILTER_JT: y = J' x (DensityFilterFun pullback). Cell-sized host arrays. */
+int tog_filter_apply(tog_handle* h, int32_t op, const double* in, double* out);
+
+/* ---- optimality-criteria update (no reference counterpart: the published OC method
+ *      with move limit and eta = 1/2, bisection on lambda in [0, 1e9] to 1e-3) ---------- */
+/* x_new = clamp(x sqrt(max(0,-dc)/(dv lambda)), max(0,x-move), min(1,x+move)) with
+ * sum(vol_weights . x_new) = volfrac.  Cell-sized host arrays. */
+int tog_oc_update(tog_handle* h, const double* x, const double* dc, const double* dv, const double* vol_weights,
+                  double volfrac, double move, double* x_new, double* change, double* lambda);
+
+/* ---- one SIMP design iteration, device-resident --------------------------------------
+ * filter -> solve -> compliance/sensitivities -> filter pullback -> OC, the loop of
+ * docs/tutorials/simp.qmd:86-114 with OC in place of MMA. */
+/* filter_kind: TOG_FILTER_NONE / DENSITY / SENS (needs rmin > 0). x0: initial design. */
+int tog_simp_init(tog_handle* h, int32_t filter_kind, double rmin, double volfrac, double move, const double* x0);
+/* precision: TOG_FP64 (cold start, as the reference) or TOG_FP32_IR; warm_start != 0
+ * starts each solve from the previous displacement. */
+int tog_simp_step(tog_handle* h, int32_t precision, double rtol, int32_t maxiter, int32_t warm_start,
+                  tog_iter_stats* stats);
+int tog_get_design(tog_handle* h, double* x);
+int tog_set_design(tog_handle* h, const double* x);
+/* Filtered (physical) densities of the last step. */
+int tog_get_physical(tog_handle* h, double* xf);
+
+/* ---- measurement hook: launch the solver's matrix-free PCG kernel n times on the
+ *      handle's stream over the handle's own PCG vectors (no host sync). ------------- */
+int tog_bench_pcg_matvec(tog_handle* h, int32_t precision, int32_t nlaunch);
+/* Algorithmic bytes moved by one launch of that kernel. */
+int tog_pcg_matvec_bytes(tog_handle* h, int32_t precision, double* bytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

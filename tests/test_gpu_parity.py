@@ -1,0 +1,207 @@
+"""GPU parity of libtopopt_gb300 against the CPU oracle, through the C ABI.
+
+Tolerances (stated per check): operator 1e-12 relative (FP64, different
+summation order); displacements 1e-8 relative at a 1e-12 solver tolerance;
+compliance 1e-6 relative and sensitivities / filtered densities 1e-5 relative
+(the accuracy bar for the SIMP path); index maps bit-exact.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+CASES_2D = [((2, 2), "mbb"), ((12, 6), "mbb"), ((60, 20), "mbb"), ((33, 10), "cant")]
+CASES_3D = [((2, 2, 2), "cant"), ((4, 2, 2), "cant"), ((7, 4, 6), "cant"), ((20, 10, 10), "cant"),
+            ((9, 4, 4), "mbb"), ((40, 16, 18), "cant")]
+
+
+def make(tg, O, nels, kind, **kw):
+    sizes = (1.0,) * len(nels)
+    if kind == "mbb":
+        return tg.HalfMBB(nels, sizes), O.half_mbb(nels, sizes)
+    return tg.PointLoadCantilever(nels, sizes, **kw), O.point_load_cantilever(nels, sizes)
+
+
+def rel(a, b):
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+@pytest.mark.parametrize("nels,kind", CASES_2D + CASES_3D)
+def test_matvec_matches_oracle(tg, O, nels, kind):
+    p, op = make(tg, O, nels, kind)
+    assert np.array_equal(p.fixed_dofs, op.fixed_dofs)
+    assert p.force_dof == op.force_dof
+    s = tg.FEASolver(tg.GB300Solver, p, xmin=1e-3, penalty=tg.PowerPenaltyFun(3.0))
+    rng = np.random.default_rng(1)
+    s.vars = rng.uniform(0.0, 1.0, p.ncells)
+    x = rng.standard_normal(p.ndofs)
+    y = s.matvec(x)
+    st = O.fea_setup(op, xmin=1e-3, p=3.0)
+    st.vars = s.vars
+    assert rel(y, O.matvec(st, x)) < 1e-12
+    s.close()
+
+
+@pytest.mark.parametrize("nels,kind", [((12, 6), "mbb"), ((60, 20), "mbb"), ((20, 10, 10), "cant"),
+                                       ((7, 4, 6), "cant")])
+@pytest.mark.parametrize("precision", ["fp64", "fp32_ir"])
+def test_solve_matches_direct(tg, O, nels, kind, precision):
+    p, op = make(tg, O, nels, kind)
+    s = tg.FEASolver(tg.GB300Solver, p, xmin=1e-3, penalty=tg.PowerPenaltyFun(3.0), rtol=1e-12, abstol=0.0,
+                     cg_max_iter=20000, precision=precision)
+    rng = np.random.default_rng(2)
+    s.vars = rng.uniform(0.2, 1.0, p.ncells)
+    s()
+    st = O.fea_setup(op, xmin=1e-3, p=3.0)
+    st.vars = s.vars
+    ud = O.direct_solve(st)
+    u = s.u
+    assert np.linalg.norm(u - ud) / np.linalg.norm(ud) < 1e-8
+    assert s.last_stats.rel_residual <= 1e-12 * 1.0001
+    s.close()
+
+
+def test_solver_agreement_reference_case(tg, O):
+    """test/FEA/solvers.jl:32-59: 20x10x10 cantilever, force -1, x = 0.5,
+    matrix-free CG vs direct within rtol 1e-4 at abstol 1e-7 (reference defaults)."""
+    import json, os
+    pin = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_pins.json")))["solver_agreement"]
+    nels = tuple(pin["nels"])
+    p = tg.PointLoadCantilever(nels, (1.0, 1.0, 1.0), 1.0, 0.3, pin["force"])
+    s = tg.FEASolver(tg.GB300Solver, p, abstol=pin["abstol"])
+    s.vars = np.full(p.ncells, pin["x"])
+    s()
+    op = O.point_load_cantilever(nels, (1.0, 1.0, 1.0), force=pin["force"])
+    st = O.fea_setup(op)
+    st.vars = s.vars
+    ud = O.direct_solve(st)
+    assert np.linalg.norm(s.u - ud) <= pin["rtol"] * np.linalg.norm(ud)
+    s.close()
+
+
+@pytest.mark.parametrize("nels,kind", [((12, 6), "mbb"), ((20, 10, 10), "cant"), ((9, 4, 4), "mbb")])
+@pytest.mark.parametrize("pen", [1.0, 2.0, 3.0])
+def test_compliance_and_sensitivities(tg, O, nels, kind, pen):
+    p, op = make(tg, O, nels, kind)
+    s = tg.FEASolver(tg.GB300Solver, p, xmin=0.01, penalty=tg.PowerPenaltyFun(pen), rtol=1e-13, abstol=0.0,
+                     cg_max_iter=20000)
+    comp = tg.ComplianceFun(s)
+    rng = np.random.default_rng(3)
+    x = np.clip(rng.random(p.ncells), 0.1, 1.0)
+    c = comp(tg.PseudoDensities(x))
+    st = O.fea_setup(op, xmin=0.01, p=pen)
+    st.vars = x
+    ud = O.direct_solve(st)
+    cr, gr, _ = O.compliance(st, ud, x)
+    assert abs(c - cr) / abs(cr) < 1e-6
+    assert rel(comp.pullback(1.0), gr) < 1e-5
+    s.close()
+
+
+@pytest.mark.parametrize("nels,kind,rmin", [((5, 5), "mbb", 2.0), ((12, 6), "mbb", 1.5), ((60, 20), "mbb", 2.0),
+                                            ((16, 8), "cant", 3.0), ((6, 4, 4), "cant", 1.5),
+                                            ((6, 4, 4), "cant", 2.0), ((8, 4, 6), "mbb", 2.5)])
+def test_filters_match_oracle(tg, O, nels, kind, rmin):
+    p, op = make(tg, O, nels, kind)
+    s = tg.FEASolver(tg.GB300Solver, p)
+    df = tg.DensityFilterFun(s, rmin)
+    sf = tg.SensFilterFun(s, rmin)
+    odf = O.DensityFilter(op, rmin)
+    rng = np.random.default_rng(4)
+    x = rng.random(p.ncells)
+    d = rng.standard_normal(p.ncells)
+    assert rel(df(tg.PseudoDensities(x)).x, odf.forward(x)) < 1e-12
+    assert rel(df.pullback(d), odf.pullback(d)) < 1e-12
+    assert np.array_equal(sf(tg.PseudoDensities(x)).x, x)
+    assert rel(sf.pullback(d), O.SensFilter(op, rmin).pullback(d)) < 1e-12
+    # uniform field preserved (test/CheqFilters/test_filters.jl:126-141)
+    assert np.allclose(df(tg.PseudoDensities(np.full(p.ncells, 0.5))).x, 0.5, rtol=1e-12)
+    s.close()
+
+
+def test_filter_too_small_rmin_raises(tg):
+    """test/CheqFilters/test_filters.jl:71-73: rmin = 0.01 throws ArgumentError."""
+    p = tg.HalfMBB((5, 5), (1.0, 1.0))
+    s = tg.FEASolver(tg.GB300Solver, p)
+    with pytest.raises(ValueError):
+        tg.DensityFilterFun(s, 0.01)
+    s.close()
+
+
+def test_oc_matches_oracle(tg, O):
+    p, op = make(tg, O, (30, 10), "mbb")
+    s = tg.FEASolver(tg.GB300Solver, p)
+    rng = np.random.default_rng(5)
+    n = p.ncells
+    x = rng.uniform(0.05, 0.95, n)
+    dc = -rng.uniform(0.0, 2.0, n)
+    dv = np.full(n, 1.0 / n)
+    w = np.full(n, 1.0 / n)
+    xn, ch, lam = tg.oc_update(s, x, dc, dv, w, 0.4, 0.2)
+    xr, chr_, lamr, _ = O.oc_update(x, dc, dv, w, 0.4, 0.2)
+    assert lam == lamr
+    assert rel(xn, xr) < 1e-14
+    assert abs(ch - chr_) < 1e-14
+    s.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32_ir"])
+def test_simp_config1_per_iteration(tg, O, precision):
+    """HalfMBB 60x20, E_min 1e-9, p = 3, V = 0.5, rmin = 2, OC move 0.2, checked
+    every design iteration on compliance (1e-6), sensitivities and filtered
+    densities (1e-5) against the oracle's direct solve.  The first 15 of the
+    100 iterations are run here to keep the test short."""
+    nels, volfrac, rmin, xmin, pen = (60, 20), 0.5, 2.0, 1e-9, 3.0
+    p, op = make(tg, O, nels, "mbb")
+    s = tg.FEASolver(tg.GB300Solver, p, xmin=xmin, penalty=tg.PowerPenaltyFun(pen), rtol=1e-10, abstol=0.0,
+                     cg_max_iter=200000, precision=precision)
+    loop = tg.SIMPLoop(s, volfrac=volfrac, rmin=rmin, filter="density")
+    st = O.fea_setup(op, xmin=xmin, p=pen)
+    filt = O.DensityFilter(op, rmin)
+    x = np.full(p.ncells, volfrac)
+    for it in range(15):
+        gst = loop.step()
+        ref = O.simp_iteration(st, x, filt, volfrac)
+        assert abs(gst.compliance - ref["c"]) / ref["c"] < 1e-6, it
+        assert rel(loop.physical, ref["xf"]) < 1e-5, it
+        assert rel(loop.x, ref["x_new"]) < 1e-5, it
+        x = loop.x      # continue from the GPU design (the per-iteration check)
+    s.close()
+
+
+def test_not_converged_status(tg):
+    p = tg.PointLoadCantilever((8, 4, 4), (1.0, 1.0, 1.0))
+    s = tg.FEASolver(tg.GB300Solver, p, rtol=1e-12, abstol=0.0, cg_max_iter=1)
+    with pytest.raises(tg.NotConverged):
+        s()
+    assert s is not None
+    s.close()
+
+
+def test_nan_vars_rejected(tg):
+    p = tg.HalfMBB((4, 2), (1.0, 1.0))
+    s = tg.FEASolver(tg.GB300Solver, p)
+    s.vars = np.full(p.ncells, np.nan)
+    with pytest.raises(tg.TopOptError):
+        s()
+    s.close()
+
+
+def test_compliance_before_solve_is_state_error(tg):
+    import ctypes
+    p = tg.HalfMBB((4, 2), (1.0, 1.0))
+    s = tg.FEASolver(tg.GB300Solver, p)
+    c = ctypes.c_double()
+    assert tg.lib().tog_compliance(s.handle, ctypes.byref(c), None) == 5
+    s.close()
+
+
+def test_singular_void_design_reports_failure(tg):
+    """All-void design with xmin = 0: K is singular; the solver must return an
+    error status (breakdown or not converged), not hang or fault."""
+    p = tg.PointLoadCantilever((6, 2, 2), (1.0, 1.0, 1.0))
+    s = tg.FEASolver(tg.GB300Solver, p, xmin=0.0, penalty=tg.PowerPenaltyFun(3.0), cg_max_iter=50)
+    s.vars = np.zeros(p.ncells)
+    with pytest.raises(tg.TopOptError):
+        s()
+    s.close()

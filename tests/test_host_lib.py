@@ -1,0 +1,70 @@
+"""The C-ABI library without a GPU: it loads, exports every symbol declared in
+include/topopt_gb300.h, and its host-only entry points (numbering, element
+stiffness) match the oracle bit-exactly / to rounding."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_symbols():
+    src = open(os.path.join(ROOT, "include", "topopt_gb300.h")).read()
+    return sorted(set(re.findall(r"^\s*(?:const char\*|int64_t|int)\s+(tog_\w+)\s*\(", src, re.M)))
+
+
+def test_library_exports_every_header_symbol(tg):
+    import ctypes
+    L = ctypes.CDLL(tg._lib.LIB_PATH)
+    syms = header_symbols()
+    assert len(syms) >= 25
+    for s in syms:
+        assert hasattr(L, s), s
+    assert set(syms) == set(tg._lib.SIGNATURES)
+    assert tg.lib().tog_version().startswith(b"libtopopt_gb300")
+
+
+@pytest.mark.parametrize("nels", [(2, 2), (5, 3), (60, 20), (160, 40), (2, 2, 2), (3, 2, 2), (5, 4, 3), (20, 10, 10)])
+def test_numbering_bit_exact(tg, O, nels):
+    """Element-to-dof maps must be bit-exact with the oracle's Ferrite restatement."""
+    g = O.rectilinear_grid(nels, (1.0,) * len(nels))
+    nd, cd = O.dof_numbering(g)
+    assert np.array_equal(tg.node_dofs(nels), nd.T)
+    assert np.array_equal(tg.cell_dofs(nels), cd.T)
+    nn, nc, ndof = tg.grid_counts(nels)
+    assert (nn, nc, ndof) == (g.nnodes, g.ncells, g.nnodes * len(nels))
+
+
+def test_problem_bcs_match_oracle(tg, O):
+    for nels in [(60, 20), (12, 6), (6, 4, 4)]:
+        p, op = tg.HalfMBB(nels, (1.0,) * len(nels)), O.half_mbb(nels, (1.0,) * len(nels))
+        assert np.array_equal(p.fixed_dofs, op.fixed_dofs) and p.force_dof == op.force_dof
+    for nels in [(160, 40), (20, 10, 10), (8, 4, 6)]:
+        p, op = tg.PointLoadCantilever(nels, (1.0,) * len(nels)), O.point_load_cantilever(nels, (1.0,) * len(nels))
+        assert np.array_equal(p.fixed_dofs, op.fixed_dofs) and p.force_dof == op.force_dof
+    p = tg.PointLoadCantilever((8, 4, 6), (1.0, 1.0, 1.0), load="face_centre")
+    op = O.point_load_cantilever((8, 4, 6), (1.0, 1.0, 1.0), load="face_centre")
+    assert p.force_dof == op.force_dof
+    with pytest.raises(ValueError):
+        tg.PointLoadCantilever((8, 3), (1.0, 1.0))
+
+
+@pytest.mark.parametrize("dim,sizes,ps", [(2, (1.0, 1.0), 0), (2, (1.0, 3.0), 0), (2, (1.0, 1.0), 1),
+                                          (3, (1.0, 1.0, 1.0), 0), (3, (1.0, 2.0, 0.5), 0)])
+def test_element_stiffness_matches_oracle(tg, O, dim, sizes, ps):
+    Ke = tg.element_stiffness(dim, sizes, 1.0, 0.3, bool(ps))
+    Ko = O.element_stiffness(dim, sizes, 1.0, 0.3, bool(ps))
+    assert np.max(np.abs(Ke - Ko)) < 1e-14 * np.max(np.abs(Ko))
+
+
+def test_host_argument_errors(tg):
+    import ctypes
+    L = tg.lib()
+    nel = (ctypes.c_int32 * 3)(2, 2, 2)
+    assert L.tog_grid_counts(4, nel, None, None, None) == 1
+    bad = (ctypes.c_int32 * 3)(0, 2, 2)
+    assert L.tog_grid_counts(3, bad, None, None, None) == 1
+    assert b"nel" in L.tog_last_error()
+    assert L.tog_destroy(None) == 0

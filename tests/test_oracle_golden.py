@@ -1,0 +1,151 @@
+"""The oracle pinned to the reference's own golden vectors and known answers
+(CPU only).  Sources: tests/golden/*.json, extracted from the TopOpt.jl test
+files by tests/golden/make_golden.py."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def load(name):
+    return json.load(open(os.path.join(GOLD, name)))
+
+
+def test_halfmbb_2x2_metadata_fixture(O):
+    """test/topopt_problems/metadata.jl:53-132."""
+    g = load("metadata_2x2.json")
+    p = O.half_mbb((2, 2), (1.0, 1.0))
+    assert p.grid.coords.tolist() == g["coords"]
+    assert (p.grid.cells + 1).tolist() == g["cells"]
+    assert (p.node_dofs + 1).tolist() == g["node_dofs"]
+    assert (p.cell_dofs + 1).tolist() == g["cell_dofs"]
+    nc = O.node_cells(p.grid)
+    for k, v in g["node_cells"].items():
+        assert [[c + 1, l + 1] for c, l in nc[int(k) - 1]] == v
+    dc = O.dof_cells(p.cell_dofs, p.ndofs)
+    for d, lst in enumerate(dc):
+        for c, l in lst:
+            assert p.cell_dofs[l, c] == d
+
+
+def test_cantilever_force_dof(O):
+    """test/topopt_problems/problems.jl:13-20."""
+    pin = load("reference_pins.json")["cantilever_force_dof"]
+    p = O.point_load_cantilever(tuple(pin["nels"]), (1.0, 1.0))
+    assert p.force_dof + 1 == pin["force_dof_1based"]
+
+
+def test_element_stiffness_properties(O):
+    for dim, sizes in [(2, (1.0, 1.0)), (3, (1.0, 1.0, 1.0)), (3, (1.0, 2.0, 0.5))]:
+        Ke = O.element_stiffness(dim, sizes, 1.0, 0.3)
+        assert np.allclose(Ke, Ke.T, atol=1e-15)
+        ev = np.linalg.eigvalsh(Ke)
+        nrigid = 3 if dim == 2 else 6
+        assert np.all(np.abs(ev[:nrigid]) < 1e-12) and np.all(ev[nrigid:] > 1e-6)
+    # plane strain = the 3D Lame constants (matrices_and_vectors.jl:83-84)
+    lam, mu = O._lame(1.0, 0.3, False)
+    assert lam == pytest.approx(1.0 * 0.3 / (1.3 * 0.4))
+    assert mu == pytest.approx(1.0 / 2.6)
+
+
+@pytest.mark.parametrize("pen", [1.0, 2.0, 3.0])
+def test_compliance_gradient_fd(O, pen):
+    """test/Functions/test_common_fns.jl:32-49: 2x2 HalfMBB, xmin 0.01, gradient vs
+    5-point central differences within 1e-5."""
+    pin = load("reference_pins.json")["compliance_fd"]
+    p = O.half_mbb(tuple(pin["nels"]), (1.0, 1.0))
+    st = O.fea_setup(p, xmin=pin["xmin"], p=pen)
+    rng = np.random.default_rng(0)
+
+    def f(x):
+        st.vars = x
+        return O.compliance(st, O.direct_solve(st), x)[0]
+
+    for _ in range(3):
+        x = np.clip(rng.random(p.grid.ncells), 0.1, 1.0)
+        st.vars = x
+        _, g, _ = O.compliance(st, O.direct_solve(st), x)
+        h = 1e-3
+        fd = np.zeros_like(x)
+        for i in range(len(x)):
+            e = np.zeros_like(x)
+            e[i] = h
+            fd[i] = (-f(x + 2 * e) + 8 * f(x + e) - 8 * f(x - e) + f(x - 2 * e)) / (12 * h)
+        assert np.linalg.norm(g - fd) <= pin["tol"]
+
+
+def test_matvec_equals_assembled_K(O):
+    for p in [O.half_mbb((5, 3), (1.0, 1.0)), O.point_load_cantilever((4, 2, 2), (1.0, 1.0, 1.0))]:
+        st = O.fea_setup(p, xmin=1e-3, p=3.0)
+        rng = np.random.default_rng(1)
+        st.vars = rng.random(p.grid.ncells)
+        x = rng.standard_normal(p.ndofs)
+        x[~st.free_mask] = 0
+        K = O.assemble(st)
+        assert np.allclose(O.matvec(st, x), K @ x, rtol=0, atol=1e-13)
+
+
+def test_solver_agreement_pcg_vs_direct(O):
+    """test/FEA/solvers.jl:32-59 (matrix-free CG vs direct, rtol 1e-4, abstol 1e-7)
+    and test/FEA/test_preconditioner.jl:147-172 (Jacobi PCG vs direct, rtol 1e-6)."""
+    pin = load("reference_pins.json")["solver_agreement"]
+    nels = tuple(pin["nels"])
+    p = O.point_load_cantilever(nels, (1.0, 1.0, 1.0), force=pin["force"])
+    st = O.fea_setup(p)
+    st.vars = np.full(p.grid.ncells, pin["x"])
+    ud = O.direct_solve(st)
+    u, it, _ = O.pcg(st, abstol=pin["abstol"], precond=False)
+    assert np.linalg.norm(u - ud) <= pin["rtol"] * np.linalg.norm(ud)
+    u, it, _ = O.pcg(st, rtol=1e-12, abstol=1e-9, maxiter=5000)
+    assert np.linalg.norm(u - ud) <= 1e-6 * np.linalg.norm(ud)
+
+
+def test_filter_identities(O):
+    """test/CheqFilters/test_filters.jl: uniform density preserved (:126-141),
+    pullback = J' (:160-198), sens filter identity forward (:200-244),
+    too-small rmin throws (:71-73)."""
+    p = O.half_mbb((5, 5), (1.0, 1.0))
+    df = O.DensityFilter(p, 2.0)
+    n = p.grid.ncells
+    assert np.allclose(df.forward(np.full(n, 0.5)), 0.5, rtol=1e-12)
+    rng = np.random.default_rng(2)
+    x, d = rng.random(n), rng.random(n)
+    assert np.isclose(d @ df.forward(x), df.pullback(d) @ x, rtol=1e-12)
+    sf = O.SensFilter(p, 2.0)
+    assert np.array_equal(sf.forward(x), x)
+    g = np.full(n, -0.3)
+    assert np.allclose(sf.pullback(g), -0.3, rtol=1e-12)
+    with pytest.raises(ValueError):
+        O.DensityFilter(p, load("reference_pins.json")["filter_too_small_rmin"]["rmin"])
+
+
+def test_filter_duplicate_node_weights(O):
+    """Each node within rmin is pushed once per traversed cell holding it
+    (CheqFilters.jl:96-101): its total weight is (rmin - d) * valence."""
+    p = O.half_mbb((6, 6), (1.0, 1.0))
+    nodes, ws = O.neighbour_info(p, 2.0)
+    ncl = O.node_cells(p.grid)
+    for i in range(p.grid.ncells):
+        agg = {}
+        for n, w in zip(nodes[i], ws[i]):
+            agg[n] = agg.get(n, 0.0) + w
+        centre = p.grid.coords[p.grid.cells[i]].mean(axis=0)
+        for n, w in agg.items():
+            d = np.linalg.norm(p.grid.coords[n] - centre)
+            assert np.isclose(w, (2.0 - d) * len(ncl[n]), rtol=1e-14)
+
+
+def test_oc_update_volume_and_bounds(O):
+    rng = np.random.default_rng(3)
+    n = 500
+    x = rng.uniform(0.05, 0.95, n)
+    dc = -rng.uniform(0.0, 1.0, n)
+    w = np.full(n, 1.0 / n)
+    xn, ch, lam, steps = O.oc_update(x, dc, w, w, 0.4, 0.2)
+    assert np.all(xn >= np.maximum(0, x - 0.2) - 1e-15) and np.all(xn <= np.minimum(1, x + 0.2) + 1e-15)
+    assert abs(w @ xn - 0.4) < 5e-3
+    assert ch == pytest.approx(np.max(np.abs(xn - x)))
+    assert steps > 10

@@ -1,0 +1,28 @@
+"""topopt.jl_gb300 -- GB300 (sm_103a) drop-in for TopOpt.jl's SIMP compliance loop.
+
+The compute path is libtopopt_gb300.so (hand-written CUDA behind a C ABI,
+include/topopt_gb300.h).  This package is its host-side mirror of the
+reference's Julia API; the Julia binding lives in julia/TopOptGB300.jl.
+Import it as ``topopt_gb300`` (see ``load()`` in the repository's
+__graft_entry__.py; the directory name carries a dot).
+"""
+from ._lib import TopOptError, NotConverged, lib  # noqa: F401
+from .topopt_api import (  # noqa: F401
+    ComplianceFun,
+    DensityFilterFun,
+    FEASolver,
+    GB300FEASolver,
+    GB300Solver,
+    HalfMBB,
+    PointLoadCantilever,
+    PowerPenaltyFun,
+    PseudoDensities,
+    SensFilterFun,
+    SIMPLoop,
+    VolumeFun,
+    cell_dofs,
+    element_stiffness,
+    grid_counts,
+    node_dofs,
+    oc_update,
+)

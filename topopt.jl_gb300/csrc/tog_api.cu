@@ -1,0 +1,1059 @@
+// C-ABI implementation of libtopopt_gb300 (see include/topopt_gb300.h).
+// One tog_handle = one structured problem resident in HBM: design, densities,
+// element scales, PCG vectors, filter stencil and OC scratch.  The per-iteration
+// host<->device traffic of the device-resident loop is a handful of scalars.
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/topopt_gb300.h"
+#include "tog_host.h"
+#include "tog_kernels.cuh"
+
+using namespace tog;
+
+namespace {
+
+thread_local std::string g_err;
+std::atomic<long long> g_launches{0};
+
+int fail(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+
+#define TOG_CUDA(call)                                                                              \
+    do {                                                                                            \
+        cudaError_t e_ = (call);                                                                    \
+        if (e_ != cudaSuccess)                                                                      \
+            return fail(e_ == cudaErrorMemoryAllocation ? TOG_ERR_OOM : TOG_ERR_CUDA,               \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                        \
+    } while (0)
+
+#define TOG_TRY(call)               \
+    do {                            \
+        int s_ = (call);            \
+        if (s_ != TOG_OK) return s_; \
+    } while (0)
+
+#define TOG_LAUNCHED(n) g_launches.fetch_add((n), std::memory_order_relaxed)
+
+constexpr int kEwThreads = 256;
+constexpr int kPcgBatch = 32;   // PCG iterations per graph launch
+constexpr int kOcMaxSteps = 100;
+
+}  // namespace
+
+struct tog_handle {
+    // problem
+    int dim = 3;
+    int32_t nel[3] = {1, 1, 1};
+    int nn[3] = {2, 2, 2};
+    long long nnodes = 0, ncells = 0, ndofs = 0;
+    double size[3] = {1, 1, 1};
+    double E = 1, nu = 0.3, xmin = 1e-3, p = 1;
+    int plane_stress = 0;
+    double meandiag = 0;
+    double fnorm2 = 0;
+    Modal<double, 3> M3d{};
+    Modal<float, 3> M3f{};
+    Modal<double, 2> M2d{};
+    Modal<float, 2> M2f{};
+    std::vector<int32_t> node_dofs;   // internal index -> reference dof
+    std::vector<int32_t> ref2int;     // reference dof -> internal index
+    // device
+    cudaStream_t own = nullptr, stream = nullptr;
+    int nsm = 152;
+    int* d_int2ref = nullptr;
+    int* d_ref2int = nullptr;
+    uint8_t* d_fixmask = nullptr;
+    double* d_f = nullptr;
+    double* d_vars = nullptr;
+    double* d_e64 = nullptr;
+    float* d_e32 = nullptr;
+    double* d_dinv64 = nullptr;
+    float* d_dinv32 = nullptr;
+    double *d_u = nullptr, *d_r64 = nullptr, *d_p64[2] = {nullptr, nullptr}, *d_q64 = nullptr;
+    float *d_x32 = nullptr, *d_r32 = nullptr, *d_p32[2] = {nullptr, nullptr}, *d_q32 = nullptr;
+    double* d_tmp = nullptr;      // dof-sized staging
+    double* d_tmp2 = nullptr;
+    double* d_cell[6] = {};       // cell-sized scratch
+    double* d_nodal = nullptr;    // node-sized scratch
+    PcgState* d_st64 = nullptr;
+    PcgState* d_st32 = nullptr;
+    OcState* d_oc = nullptr;
+    double* d_partials = nullptr;
+    size_t npartials = 0;
+    unsigned* d_cnt = nullptr;    // misc counters
+    double* d_scalar = nullptr;   // misc results
+    PcgState* h_st = nullptr;     // pinned
+    OcState* h_oc = nullptr;
+    double* h_scalar = nullptr;
+    // filter
+    int* d_soff = nullptr;
+    double* d_sw = nullptr;
+    int S = 0;
+    double* d_invW = nullptr;
+    bool filter_ready = false;
+    double rmin = 0;
+    // state
+    bool vars_dirty = true;
+    bool u_valid = false;
+    // SIMP loop
+    int simp_filter = TOG_FILTER_NONE;
+    double volfrac = 0.5, move = 0.2;
+    double *d_x = nullptr, *d_xnew = nullptr, *d_dc = nullptr, *d_dv = nullptr, *d_w = nullptr, *d_grad = nullptr,
+           *d_B = nullptr;
+    bool simp_ready = false;
+    // graphs
+    cudaGraphExec_t g_pcg64 = nullptr, g_pcg32 = nullptr, g_oc = nullptr;
+    int graph_nodes_pcg = 0;
+
+    Dims dims() const {
+        Dims D;
+        D.dim = dim;
+        for (int d = 0; d < 3; ++d) {
+            D.nel[d] = d < dim ? nel[d] : 1;
+            D.nn[d] = d < dim ? nn[d] : 1;
+        }
+        D.nnodes = nnodes;
+        D.ncells = ncells;
+        return D;
+    }
+    int ew_blocks(long long n) const {
+        long long b = (n + kEwThreads - 1) / kEwThreads;
+        long long cap = (long long)nsm * 8;
+        if (b > cap) b = cap;
+        if (b < 1) b = 1;
+        return (int)b;
+    }
+};
+
+namespace {
+
+template <typename T>
+int dalloc(T** p, size_t n) {
+    cudaError_t e = cudaMalloc((void**)p, n * sizeof(T) + 16);
+    if (e != cudaSuccess) return fail(TOG_ERR_OOM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    return TOG_OK;
+}
+
+dim3 mv3_grid(const tog_handle* h) {
+    return dim3((h->nn[0] + 30) / 31, (h->nn[1] + MV_BY - 2) / (MV_BY - 1), (h->nn[2] + MV_LZ - 1) / MV_LZ);
+}
+dim3 mv2_grid(const tog_handle* h) {
+    const int chunks = (h->nn[1] + MV2_LY - 1) / MV2_LY;
+    return dim3((h->nn[0] + 30) / 31, (chunks + MV2_WARPS - 1) / MV2_WARPS, 1);
+}
+
+template <typename T>
+MvArgs<T, 3> mv_args3(tog_handle* h);
+template <>
+MvArgs<double, 3> mv_args3<double>(tog_handle* h) {
+    MvArgs<double, 3> A{};
+    A.escale = h->d_e64;
+    A.dinv = h->d_dinv64;
+    A.r = h->d_r64;
+    A.P0 = h->d_p64[0];
+    A.P1 = h->d_p64[1];
+    A.q = h->d_q64;
+    A.st = h->d_st64;
+    A.M = h->M3d;
+    return A;
+}
+template <>
+MvArgs<float, 3> mv_args3<float>(tog_handle* h) {
+    MvArgs<float, 3> A{};
+    A.escale = h->d_e32;
+    A.dinv = h->d_dinv32;
+    A.r = h->d_r32;
+    A.P0 = h->d_p32[0];
+    A.P1 = h->d_p32[1];
+    A.q = h->d_q32;
+    A.st = h->d_st32;
+    A.M = h->M3f;
+    return A;
+}
+template <typename T>
+MvArgs<T, 2> mv_args2(tog_handle* h);
+template <>
+MvArgs<double, 2> mv_args2<double>(tog_handle* h) {
+    MvArgs<double, 2> A{};
+    A.escale = h->d_e64;
+    A.dinv = h->d_dinv64;
+    A.r = h->d_r64;
+    A.P0 = h->d_p64[0];
+    A.P1 = h->d_p64[1];
+    A.q = h->d_q64;
+    A.st = h->d_st64;
+    A.M = h->M2d;
+    return A;
+}
+template <>
+MvArgs<float, 2> mv_args2<float>(tog_handle* h) {
+    MvArgs<float, 2> A{};
+    A.escale = h->d_e32;
+    A.dinv = h->d_dinv32;
+    A.r = h->d_r32;
+    A.P0 = h->d_p32[0];
+    A.P1 = h->d_p32[1];
+    A.q = h->d_q32;
+    A.st = h->d_st32;
+    A.M = h->M2f;
+    return A;
+}
+
+template <typename T, int DIM>
+void fill_common(tog_handle* h, MvArgs<T, DIM>& A) {
+    A.fixmask = h->d_fixmask;
+    A.meandiag = (T)h->meandiag;
+    for (int d = 0; d < 3; ++d) {
+        A.nel[d] = d < h->dim ? h->nel[d] : 1;
+        A.nn[d] = d < h->dim ? h->nn[d] : 1;
+    }
+    A.partials = h->d_partials;
+}
+
+// Launch one matrix-free operator kernel (mode MV_*) in precision T.
+template <typename T, int MODE>
+void launch_matvec(tog_handle* h, cudaStream_t s, const T* x, T* y, const double* f) {
+    if (h->dim == 3) {
+        MvArgs<T, 3> A = mv_args3<T>(h);
+        fill_common<T, 3>(h, A);
+        A.x = x;
+        A.y = y;
+        A.f = f;
+        if (MODE == MV_RESID) A.st = h->d_st64;
+        k_matvec3<T, MODE><<<mv3_grid(h), dim3(32, MV_BY), 0, s>>>(A);
+    } else {
+        MvArgs<T, 2> A = mv_args2<T>(h);
+        fill_common<T, 2>(h, A);
+        A.x = x;
+        A.y = y;
+        A.f = f;
+        if (MODE == MV_RESID) A.st = h->d_st64;
+        k_matvec2<T, MODE><<<mv2_grid(h), dim3(32, MV2_WARPS), 0, s>>>(A);
+    }
+    TOG_LAUNCHED(1);
+}
+
+template <typename T>
+void launch_pcg_update(tog_handle* h, cudaStream_t s) {
+    const int nb = h->ew_blocks(h->nnodes);
+    if (std::is_same<T, double>::value) {
+        if (h->dim == 3)
+            k_pcg_update<double, 3><<<nb, kEwThreads, 0, s>>>(h->d_u, h->d_r64, h->d_p64[0], h->d_p64[1], h->d_q64,
+                                                              h->d_dinv64, h->M3d, h->nnodes, h->d_st64,
+                                                              h->d_partials);
+        else
+            k_pcg_update<double, 2><<<nb, kEwThreads, 0, s>>>(h->d_u, h->d_r64, h->d_p64[0], h->d_p64[1], h->d_q64,
+                                                              h->d_dinv64, h->M2d, h->nnodes, h->d_st64,
+                                                              h->d_partials);
+    } else {
+        if (h->dim == 3)
+            k_pcg_update<float, 3><<<nb, kEwThreads, 0, s>>>(h->d_x32, h->d_r32, h->d_p32[0], h->d_p32[1], h->d_q32,
+                                                             h->d_dinv32, h->M3f, h->nnodes, h->d_st32,
+                                                             h->d_partials);
+        else
+            k_pcg_update<float, 2><<<nb, kEwThreads, 0, s>>>(h->d_x32, h->d_r32, h->d_p32[0], h->d_p32[1], h->d_q32,
+                                                             h->d_dinv32, h->M2f, h->nnodes, h->d_st32,
+                                                             h->d_partials);
+    }
+    TOG_LAUNCHED(1);
+}
+
+template <typename T>
+void launch_pcg_init(tog_handle* h, cudaStream_t s, int zero_x, double rtol, double abstol, double bnorm2, int maxit) {
+    const int nb = h->ew_blocks(h->nnodes);
+    if (std::is_same<T, double>::value) {
+        if (h->dim == 3)
+            k_pcg_init<double, 3><<<nb, kEwThreads, 0, s>>>(h->d_u, h->d_r64, h->d_p64[0], h->d_p64[1], h->d_dinv64,
+                                                            h->M3d, h->nnodes, zero_x, rtol, abstol, bnorm2, maxit,
+                                                            h->d_st64, h->d_partials);
+        else
+            k_pcg_init<double, 2><<<nb, kEwThreads, 0, s>>>(h->d_u, h->d_r64, h->d_p64[0], h->d_p64[1], h->d_dinv64,
+                                                            h->M2d, h->nnodes, zero_x, rtol, abstol, bnorm2, maxit,
+                                                            h->d_st64, h->d_partials);
+    } else {
+        if (h->dim == 3)
+            k_pcg_init<float, 3><<<nb, kEwThreads, 0, s>>>(h->d_x32, h->d_r32, h->d_p32[0], h->d_p32[1],
+                                                           h->d_dinv32, h->M3f, h->nnodes, zero_x, rtol, abstol,
+                                                           bnorm2, maxit, h->d_st32, h->d_partials);
+        else
+            k_pcg_init<float, 2><<<nb, kEwThreads, 0, s>>>(h->d_x32, h->d_r32, h->d_p32[0], h->d_p32[1],
+                                                           h->d_dinv32, h->M2f, h->nnodes, zero_x, rtol, abstol,
+                                                           bnorm2, maxit, h->d_st32, h->d_partials);
+    }
+    TOG_LAUNCHED(1);
+}
+
+// Graph of kPcgBatch PCG iterations (operator + update per iteration).  Kernels
+// read the iteration state from device memory and return at once after
+// convergence, so one graph serves every batch of every solve.
+template <typename T>
+int build_pcg_graph(tog_handle* h, cudaGraphExec_t* out) {
+    cudaGraph_t g = nullptr;
+    TOG_CUDA(cudaStreamBeginCapture(h->own, cudaStreamCaptureModeThreadLocal));
+    for (int i = 0; i < kPcgBatch; ++i) {
+        launch_matvec<T, MV_PCG>(h, h->own, nullptr, nullptr, nullptr);
+        launch_pcg_update<T>(h, h->own);
+    }
+    TOG_LAUNCHED(-2 * kPcgBatch);   // counted when the graph is launched
+    TOG_CUDA(cudaStreamEndCapture(h->own, &g));
+    TOG_CUDA(cudaGraphInstantiate(out, g, 0));
+    cudaGraphDestroy(g);
+    return TOG_OK;
+}
+
+int sync_state(tog_handle* h, const PcgState* d_st) {
+    TOG_CUDA(cudaMemcpyAsync(h->h_st, d_st, sizeof(PcgState), cudaMemcpyDeviceToHost, h->stream));
+    TOG_CUDA(cudaStreamSynchronize(h->stream));
+    return TOG_OK;
+}
+
+// Run graph batches until the PCG state says done.
+template <typename T>
+int run_pcg(tog_handle* h) {
+    cudaGraphExec_t* g = std::is_same<T, double>::value ? &h->g_pcg64 : &h->g_pcg32;
+    PcgState* d_st = std::is_same<T, double>::value ? h->d_st64 : h->d_st32;
+    if (!*g) TOG_TRY(build_pcg_graph<T>(h, g));
+    TOG_TRY(sync_state(h, d_st));
+    while (!h->h_st->done) {
+        TOG_CUDA(cudaGraphLaunch(*g, h->stream));
+        TOG_LAUNCHED(2 * kPcgBatch);
+        TOG_TRY(sync_state(h, d_st));
+    }
+    return TOG_OK;
+}
+
+int refresh_scales(tog_handle* h) {
+    if (!h->vars_dirty) return TOG_OK;
+    double ip_f = std::floor(h->p);
+    const int ip = (h->p == ip_f && h->p >= 0 && h->p <= 8) ? (int)ip_f : -1;
+    k_escale<<<h->ew_blocks(h->ncells), kEwThreads, 0, h->stream>>>(h->d_vars, h->d_e64, h->d_e32, h->ncells,
+                                                                   h->xmin, h->p, ip);
+    TOG_LAUNCHED(1);
+    if (h->dim == 3)
+        k_nodesum<3><<<h->ew_blocks(h->nnodes), kEwThreads, 0, h->stream>>>(h->d_e64, h->d_dinv64, h->d_dinv32,
+                                                                            h->dims());
+    else
+        k_nodesum<2><<<h->ew_blocks(h->nnodes), kEwThreads, 0, h->stream>>>(h->d_e64, h->d_dinv64, h->d_dinv32,
+                                                                            h->dims());
+    TOG_LAUNCHED(1);
+    TOG_CUDA(cudaGetLastError());
+    h->vars_dirty = false;
+    return TOG_OK;
+}
+
+int solve_fp64(tog_handle* h, double rtol, double abstol, int maxit, int warm, tog_solve_stats* st) {
+    if (warm && h->u_valid) {
+        launch_matvec<double, MV_RESID>(h, h->stream, h->d_u, h->d_r64, h->d_f);
+        launch_pcg_init<double>(h, h->stream, 0, rtol, abstol, h->fnorm2, maxit);
+    } else {
+        TOG_CUDA(cudaMemcpyAsync(h->d_r64, h->d_f, h->ndofs * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+        launch_pcg_init<double>(h, h->stream, 1, rtol, abstol, h->fnorm2, maxit);
+    }
+    TOG_CUDA(cudaGetLastError());
+    TOG_TRY(run_pcg<double>(h));
+    h->u_valid = true;
+    const PcgState& s = *h->h_st;
+    if (st) {
+        st->status = s.status;
+        st->iterations = s.it;
+        st->outer_iterations = 0;
+        st->abs_residual = std::sqrt(s.rr);
+        st->rel_residual = h->fnorm2 > 0 ? std::sqrt(s.rr / h->fnorm2) : std::sqrt(s.rr);
+    }
+    return s.status == 0 ? TOG_OK : fail(s.status, s.status == 3 ? "PCG did not converge within maxiter"
+                                                                   : "PCG breakdown (p'Kp <= 0 or NaN)");
+}
+
+int solve_fp32_ir(tog_handle* h, double rtol, double abstol, int maxit, int warm, tog_solve_stats* st) {
+    const long long nd = h->ndofs;
+    if (!(warm && h->u_valid)) TOG_CUDA(cudaMemsetAsync(h->d_u, 0, nd * sizeof(double), h->stream));
+    const double tol = std::fmax(rtol * std::sqrt(h->fnorm2), abstol);
+    int inner_total = 0, outer = 0, status = TOG_OK;
+    double res = 0.0;
+    const int max_outer = 60;
+    for (;;) {
+        // FP64 true residual r = f - K u
+        launch_matvec<double, MV_RESID>(h, h->stream, h->d_u, h->d_r64, h->d_f);
+        TOG_CUDA(cudaGetLastError());
+        TOG_TRY(sync_state(h, h->d_st64));
+        res = std::sqrt(h->h_st->rr);
+        if (!std::isfinite(res)) {
+            status = TOG_BREAKDOWN;
+            break;
+        }
+        if (res <= tol) break;
+        if (outer >= max_outer || inner_total >= maxit) {
+            status = TOG_NOT_CONVERGED;
+            break;
+        }
+        // inner FP32 solve of K d = r / ||r|| to relative tolerance eta
+        const double need = tol / res;
+        const double eta = std::fmin(0.5, std::fmax(1e-4, 0.3 * need));
+        const int nb = h->ew_blocks(nd);
+        if (h->dim == 3)
+            k_ir_scale<3><<<nb, kEwThreads, 0, h->stream>>>(h->d_r64, h->d_r32, nd, h->d_st64);
+        else
+            k_ir_scale<2><<<nb, kEwThreads, 0, h->stream>>>(h->d_r64, h->d_r32, nd, h->d_st64);
+        TOG_LAUNCHED(1);
+        launch_pcg_init<float>(h, h->stream, 1, eta, 0.0, -1.0, maxit - inner_total);
+        TOG_CUDA(cudaGetLastError());
+        TOG_TRY(run_pcg<float>(h));
+        const int its = h->h_st->it;
+        const int ist = h->h_st->status;
+        inner_total += its;
+        k_ir_correct<<<nb, kEwThreads, 0, h->stream>>>(h->d_u, h->d_x32, nd, h->d_st64);
+        TOG_LAUNCHED(1);
+        ++outer;
+        if (ist == 4 && its == 0) {
+            status = TOG_BREAKDOWN;
+            break;
+        }
+    }
+    h->u_valid = true;
+    if (st) {
+        st->status = status;
+        st->iterations = inner_total;
+        st->outer_iterations = outer;
+        st->abs_residual = res;
+        st->rel_residual = h->fnorm2 > 0 ? res / std::sqrt(h->fnorm2) : res;
+    }
+    if (status == TOG_NOT_CONVERGED) return fail(status, "FP32-IR did not reach the FP64 tolerance");
+    if (status == TOG_BREAKDOWN) return fail(status, "FP32-IR breakdown");
+    return TOG_OK;
+}
+
+int do_solve(tog_handle* h, int prec, double rtol, double abstol, int maxit, int warm, tog_solve_stats* st) {
+    TOG_TRY(refresh_scales(h));
+    if (prec == TOG_FP64) return solve_fp64(h, rtol, abstol, maxit, warm, st);
+    if (prec == TOG_FP32_IR) return solve_fp32_ir(h, rtol, abstol, maxit, warm, st);
+    return fail(TOG_ERR_ARG, "unknown precision");
+}
+
+int compliance_dev(tog_handle* h, double* d_grad) {
+    const int nb = h->ew_blocks(h->ncells);
+    double ip_f = std::floor(h->p);
+    const int ip = (h->p == ip_f && h->p >= 0 && h->p <= 8) ? (int)ip_f : -1;
+    if (h->dim == 3)
+        k_compliance<3><<<nb, kEwThreads, 0, h->stream>>>(h->d_u, h->d_vars, h->M3d, h->xmin, h->p, ip, h->dims(),
+                                                          d_grad, nullptr, h->d_partials, h->d_cnt, h->d_scalar);
+    else
+        k_compliance<2><<<nb, kEwThreads, 0, h->stream>>>(h->d_u, h->d_vars, h->M2d, h->xmin, h->p, ip, h->dims(),
+                                                          d_grad, nullptr, h->d_partials, h->d_cnt, h->d_scalar);
+    TOG_LAUNCHED(1);
+    TOG_CUDA(cudaGetLastError());
+    return TOG_OK;
+}
+
+// y = J x (op 0) or J' x (op 1), device arrays
+int filter_dev(tog_handle* h, int op, const double* in, double* out) {
+    const Dims D = h->dims();
+    const int nbn = h->ew_blocks(h->nnodes), nbc = h->ew_blocks(h->ncells);
+    cudaStream_t s = h->stream;
+    if (op == TOG_FILTER_J) {
+        if (h->dim == 3) {
+            k_filt_node_avg<3><<<nbn, kEwThreads, 0, s>>>(in, h->d_nodal, D);
+            k_filt_cone<3><<<nbc, kEwThreads, 0, s>>>(h->d_nodal, out, h->d_soff, h->d_sw, h->S, h->d_invW, in, D);
+        } else {
+            k_filt_node_avg<2><<<nbn, kEwThreads, 0, s>>>(in, h->d_nodal, D);
+            k_filt_cone<2><<<nbc, kEwThreads, 0, s>>>(h->d_nodal, out, h->d_soff, h->d_sw, h->S, h->d_invW, in, D);
+        }
+    } else {
+        if (h->dim == 3) {
+            k_filt_cone_T<3><<<nbn, kEwThreads, 0, s>>>(in, h->d_nodal, h->d_soff, h->d_sw, h->S, h->d_invW, D);
+            k_filt_node_avg_T<3><<<nbc, kEwThreads, 0, s>>>(h->d_nodal, out, D);
+        } else {
+            k_filt_cone_T<2><<<nbn, kEwThreads, 0, s>>>(in, h->d_nodal, h->d_soff, h->d_sw, h->S, h->d_invW, D);
+            k_filt_node_avg_T<2><<<nbc, kEwThreads, 0, s>>>(h->d_nodal, out, D);
+        }
+    }
+    TOG_LAUNCHED(2);
+    TOG_CUDA(cudaGetLastError());
+    return TOG_OK;
+}
+
+int build_oc_graph(tog_handle* h) {
+    cudaGraph_t g = nullptr;
+    TOG_CUDA(cudaStreamBeginCapture(h->own, cudaStreamCaptureModeThreadLocal));
+    const int nb = h->ew_blocks(h->ncells);
+    for (int i = 0; i < kOcMaxSteps; ++i)
+        k_oc_step<<<nb, kEwThreads, 0, h->own>>>(h->d_x, h->d_B, h->d_w, h->ncells, h->d_oc, h->d_partials);
+    k_oc_final<<<nb, kEwThreads, 0, h->own>>>(h->d_x, h->d_B, h->d_xnew, h->ncells, h->d_oc, h->d_partials,
+                                               h->d_w);
+    TOG_CUDA(cudaStreamEndCapture(h->own, &g));
+    TOG_CUDA(cudaGraphInstantiate(&h->g_oc, g, 0));
+    cudaGraphDestroy(g);
+    return TOG_OK;
+}
+
+// OC on the device arrays d_x, d_dc, d_dv, d_w -> d_xnew
+int oc_dev(tog_handle* h, double volfrac, double move) {
+    if (!h->g_oc) TOG_TRY(build_oc_graph(h));
+    const int nb = h->ew_blocks(h->ncells);
+    k_oc_prep<<<nb, kEwThreads, 0, h->stream>>>(h->d_x, h->d_dc, h->d_dv, h->d_B, h->ncells, h->d_oc, 0.0, 1e9, 1e-3,
+                                                volfrac, move, kOcMaxSteps);
+    TOG_LAUNCHED(1);
+    TOG_CUDA(cudaGetLastError());
+    TOG_CUDA(cudaGraphLaunch(h->g_oc, h->stream));
+    TOG_LAUNCHED(kOcMaxSteps + 1);
+    TOG_CUDA(cudaMemcpyAsync(h->h_oc, h->d_oc, sizeof(OcState), cudaMemcpyDeviceToHost, h->stream));
+    TOG_CUDA(cudaStreamSynchronize(h->stream));
+    return TOG_OK;
+}
+
+int upload_dofs(tog_handle* h, const double* ref, double* d_internal) {
+    TOG_CUDA(cudaMemcpyAsync(h->d_tmp2, ref, h->ndofs * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    k_gather_d<<<h->ew_blocks(h->ndofs), kEwThreads, 0, h->stream>>>(h->d_tmp2, h->d_int2ref, d_internal, h->ndofs);
+    TOG_LAUNCHED(1);
+    TOG_CUDA(cudaGetLastError());
+    return TOG_OK;
+}
+int download_dofs(tog_handle* h, const double* d_internal, double* ref) {
+    k_gather_d<<<h->ew_blocks(h->ndofs), kEwThreads, 0, h->stream>>>(d_internal, h->d_ref2int, h->d_tmp2, h->ndofs);
+    TOG_LAUNCHED(1);
+    TOG_CUDA(cudaGetLastError());
+    TOG_CUDA(cudaMemcpyAsync(ref, h->d_tmp2, h->ndofs * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    TOG_CUDA(cudaStreamSynchronize(h->stream));
+    return TOG_OK;
+}
+
+int check_handle(tog_handle* h) {
+    if (!h) return fail(TOG_ERR_ARG, "null handle");
+    return TOG_OK;
+}
+
+}  // namespace
+
+// ============================================================================
+// C ABI
+// ============================================================================
+extern "C" {
+
+const char* tog_version(void) { return "libtopopt_gb300 1 (sm_103a)"; }
+const char* tog_last_error(void) { return g_err.c_str(); }
+int64_t tog_launch_count(void) { return g_launches.load(); }
+
+int tog_grid_counts(int32_t dim, const int32_t* nel, int64_t* nnodes, int64_t* ncells, int64_t* ndofs) {
+    if ((dim != 2 && dim != 3) || !nel) return fail(TOG_ERR_ARG, "dim must be 2 or 3");
+    for (int d = 0; d < dim; ++d)
+        if (nel[d] < 1) return fail(TOG_ERR_ARG, "nel must be >= 1");
+    long long nn, nc;
+    grid_counts(dim, nel, &nn, &nc);
+    if (nnodes) *nnodes = nn;
+    if (ncells) *ncells = nc;
+    if (ndofs) *ndofs = nn * dim;
+    return TOG_OK;
+}
+
+int tog_node_dofs(int32_t dim, const int32_t* nel, int32_t* node_dofs) {
+    TOG_TRY(tog_grid_counts(dim, nel, nullptr, nullptr, nullptr));
+    if (!node_dofs) return fail(TOG_ERR_ARG, "null output");
+    node_dofs_first_touch(dim, nel, node_dofs);
+    return TOG_OK;
+}
+
+int tog_cell_dofs(int32_t dim, const int32_t* nel, int32_t* cell_dofs) {
+    int64_t nn;
+    TOG_TRY(tog_grid_counts(dim, nel, &nn, nullptr, nullptr));
+    if (!cell_dofs) return fail(TOG_ERR_ARG, "null output");
+    std::vector<int32_t> nd((size_t)nn * dim);
+    node_dofs_first_touch(dim, nel, nd.data());
+    cell_dofs_from_node_dofs(dim, nel, nd.data(), cell_dofs);
+    return TOG_OK;
+}
+
+int tog_element_stiffness(int32_t dim, const double* size, double E, double nu, int32_t plane_stress, double* Ke) {
+    if ((dim != 2 && dim != 3) || !size || !Ke) return fail(TOG_ERR_ARG, "bad arguments");
+    if (!(nu > -1.0 && nu < 0.5) || !(E > 0)) return fail(TOG_ERR_ARG, "need E > 0 and -1 < nu < 0.5");
+    element_stiffness(dim, size, E, nu, plane_stress, Ke);
+    return TOG_OK;
+}
+
+int tog_create(const tog_problem_desc* desc, tog_handle** out) {
+    if (!desc || !out) return fail(TOG_ERR_ARG, "null argument");
+    *out = nullptr;
+    const int dim = desc->dim;
+    TOG_TRY(tog_grid_counts(dim, desc->nel, nullptr, nullptr, nullptr));
+    for (int d = 0; d < dim; ++d)
+        if (!(desc->size[d] > 0)) return fail(TOG_ERR_ARG, "element sizes must be > 0");
+    if (!(desc->E > 0) || !(desc->nu > -1.0 && desc->nu < 0.5)) return fail(TOG_ERR_ARG, "need E > 0 and -1 < nu < 0.5");
+    if (!(desc->xmin >= 0 && desc->xmin < 1)) return fail(TOG_ERR_ARG, "xmin must be in [0, 1)");
+    tog_handle* h = new tog_handle();
+    h->dim = dim;
+    for (int d = 0; d < 3; ++d) {
+        h->nel[d] = d < dim ? desc->nel[d] : 1;
+        h->nn[d] = d < dim ? desc->nel[d] + 1 : 1;
+        h->size[d] = d < dim ? desc->size[d] : 1.0;
+    }
+    grid_counts(dim, desc->nel, &h->nnodes, &h->ncells);
+    h->ndofs = h->nnodes * dim;
+    if (h->ndofs >= (1LL << 31)) {
+        delete h;
+        return fail(TOG_ERR_ARG, "more than 2^31 dofs");
+    }
+    h->E = desc->E;
+    h->nu = desc->nu;
+    h->xmin = desc->xmin;
+    h->p = desc->penalty;
+    h->plane_stress = desc->plane_stress;
+    // numbering
+    h->node_dofs.resize(h->ndofs);
+    node_dofs_first_touch(dim, desc->nel, h->node_dofs.data());
+    h->ref2int.assign(h->ndofs, -1);
+    for (long long i = 0; i < h->ndofs; ++i) h->ref2int[h->node_dofs[i]] = (int32_t)i;
+    // element operator
+    const int nd = (1 << dim) * dim;
+    std::vector<double> Ke(nd * nd);
+    element_stiffness(dim, h->size, h->E, h->nu, h->plane_stress, Ke.data());
+    double tr = 0;
+    for (int i = 0; i < nd; ++i) tr += Ke[i * nd + i];
+    h->meandiag = tr * (double)h->ncells;   // sum of element traces (solvers_api.jl:526-527)
+    double kd[3];
+    try {
+        if (dim == 3) {
+            modal_operator(3, Ke.data(), &h->M3d.D[0][0], &h->M3d.O[0][0][0], kd);
+            for (int m = 0; m < 8; ++m)
+                for (int c = 0; c < 3; ++c) {
+                    h->M3f.D[m][c] = (float)h->M3d.D[m][c];
+                    for (int d = 0; d < 3; ++d) h->M3f.O[m][c][d] = (float)h->M3d.O[m][c][d];
+                }
+            for (int c = 0; c < 3; ++c) {
+                h->M3d.kdinv[c] = 1.0 / kd[c];
+                h->M3f.kdinv[c] = (float)(1.0 / kd[c]);
+            }
+        } else {
+            modal_operator(2, Ke.data(), &h->M2d.D[0][0], &h->M2d.O[0][0][0], kd);
+            for (int m = 0; m < 4; ++m)
+                for (int c = 0; c < 2; ++c) {
+                    h->M2f.D[m][c] = (float)h->M2d.D[m][c];
+                    for (int d = 0; d < 2; ++d) h->M2f.O[m][c][d] = (float)h->M2d.O[m][c][d];
+                }
+            for (int c = 0; c < 2; ++c) {
+                h->M2d.kdinv[c] = 1.0 / kd[c];
+                h->M2f.kdinv[c] = (float)(1.0 / kd[c]);
+            }
+        }
+    } catch (const std::exception& ex) {
+        delete h;
+        return fail(TOG_ERR_ARG, ex.what());
+    }
+    // device
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&h->nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->own, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete h;
+        return fail(TOG_ERR_CUDA, std::string("CUDA init: ") + cudaGetErrorString(e));
+    }
+    h->stream = h->own;
+    const long long N = h->ndofs, NN = h->nnodes, NC = h->ncells;
+    // partial-sum buffer: enough for the largest grid of any reducing kernel
+    const dim3 g3 = mv3_grid(h), g2 = mv2_grid(h);
+    size_t maxb = (size_t)g3.x * g3.y * g3.z;
+    maxb = std::max(maxb, (size_t)g2.x * g2.y);
+    maxb = std::max(maxb, (size_t)h->nsm * 8);
+    h->npartials = maxb * 4;
+    int rc = TOG_OK;
+    auto A = [&](int r) {
+        if (rc == TOG_OK) rc = r;
+    };
+    A(dalloc(&h->d_int2ref, N));
+    A(dalloc(&h->d_ref2int, N));
+    A(dalloc(&h->d_fixmask, NN));
+    A(dalloc(&h->d_f, N));
+    A(dalloc(&h->d_vars, NC));
+    A(dalloc(&h->d_e64, NC));
+    A(dalloc(&h->d_e32, NC));
+    A(dalloc(&h->d_dinv64, NN));
+    A(dalloc(&h->d_dinv32, NN));
+    A(dalloc(&h->d_u, N));
+    A(dalloc(&h->d_r64, N));
+    A(dalloc(&h->d_p64[0], N));
+    A(dalloc(&h->d_p64[1], N));
+    A(dalloc(&h->d_q64, N));
+    A(dalloc(&h->d_x32, N));
+    A(dalloc(&h->d_r32, N));
+    A(dalloc(&h->d_p32[0], N));
+    A(dalloc(&h->d_p32[1], N));
+    A(dalloc(&h->d_q32, N));
+    A(dalloc(&h->d_tmp, N));
+    A(dalloc(&h->d_tmp2, N));
+    for (int i = 0; i < 6; ++i) A(dalloc(&h->d_cell[i], NC));
+    A(dalloc(&h->d_nodal, NN));
+    A(dalloc(&h->d_st64, 1));
+    A(dalloc(&h->d_st32, 1));
+    A(dalloc(&h->d_oc, 1));
+    A(dalloc(&h->d_partials, h->npartials));
+    A(dalloc(&h->d_cnt, 8));
+    A(dalloc(&h->d_scalar, 8));
+    A(dalloc(&h->d_invW, NC));
+    if (rc == TOG_OK) {
+        h->d_x = h->d_cell[0];
+        h->d_xnew = h->d_cell[1];
+        h->d_dc = h->d_cell[2];
+        h->d_dv = h->d_cell[3];
+        h->d_w = h->d_cell[4];
+        h->d_grad = h->d_cell[5];
+        h->d_B = h->d_tmp;   // OC scratch shares the dof staging buffer (ncells <= ndofs)
+        cudaError_t ee = cudaSuccess;
+        auto C = [&](cudaError_t x) {
+            if (ee == cudaSuccess) ee = x;
+        };
+        C(cudaHostAlloc((void**)&h->h_st, sizeof(PcgState), cudaHostAllocDefault));
+        C(cudaHostAlloc((void**)&h->h_oc, sizeof(OcState), cudaHostAllocDefault));
+        C(cudaHostAlloc((void**)&h->h_scalar, 8 * sizeof(double), cudaHostAllocDefault));
+        C(cudaMemcpyAsync(h->d_int2ref, h->node_dofs.data(), N * sizeof(int), cudaMemcpyHostToDevice, h->own));
+        C(cudaMemcpyAsync(h->d_ref2int, h->ref2int.data(), N * sizeof(int), cudaMemcpyHostToDevice, h->own));
+        C(cudaMemsetAsync(h->d_fixmask, 0, NN, h->own));
+        C(cudaMemsetAsync(h->d_f, 0, N * sizeof(double), h->own));
+        C(cudaMemsetAsync(h->d_u, 0, N * sizeof(double), h->own));
+        C(cudaMemsetAsync(h->d_st64, 0, sizeof(PcgState), h->own));
+        C(cudaMemsetAsync(h->d_st32, 0, sizeof(PcgState), h->own));
+        C(cudaMemsetAsync(h->d_oc, 0, sizeof(OcState), h->own));
+        C(cudaMemsetAsync(h->d_cnt, 0, 8 * sizeof(unsigned), h->own));
+        // vars = ones (solvers_api.jl:502)
+        std::vector<double> ones(NC, 1.0);
+        C(cudaMemcpyAsync(h->d_vars, ones.data(), NC * sizeof(double), cudaMemcpyHostToDevice, h->own));
+        C(cudaStreamSynchronize(h->own));
+        if (ee != cudaSuccess) rc = fail(TOG_ERR_CUDA, std::string("init: ") + cudaGetErrorString(ee));
+    }
+    if (rc != TOG_OK) {
+        std::string msg = g_err;
+        tog_destroy(h);
+        g_err = msg;
+        return rc;
+    }
+    h->vars_dirty = true;
+    *out = h;
+    return TOG_OK;
+}
+
+int tog_destroy(tog_handle* h) {
+    if (!h) return TOG_OK;
+    if (h->own) cudaStreamSynchronize(h->own);
+    if (h->stream && h->stream != h->own) cudaStreamSynchronize(h->stream);
+    if (h->g_pcg64) cudaGraphExecDestroy(h->g_pcg64);
+    if (h->g_pcg32) cudaGraphExecDestroy(h->g_pcg32);
+    if (h->g_oc) cudaGraphExecDestroy(h->g_oc);
+    void* ptrs[] = {h->d_int2ref, h->d_ref2int, h->d_fixmask, h->d_f,   h->d_vars,  h->d_e64,    h->d_e32,
+                    h->d_dinv64,  h->d_dinv32,  h->d_u,       h->d_r64, h->d_p64[0], h->d_p64[1], h->d_q64,
+                    h->d_x32,     h->d_r32,     h->d_p32[0],  h->d_p32[1], h->d_q32, h->d_tmp,    h->d_tmp2,
+                    h->d_nodal,   h->d_st64,    h->d_st32,    h->d_oc,  h->d_partials, h->d_cnt,  h->d_scalar,
+                    h->d_invW,    h->d_soff,    h->d_sw};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    for (int i = 0; i < 6; ++i)
+        if (h->d_cell[i]) cudaFree(h->d_cell[i]);
+    if (h->h_st) cudaFreeHost(h->h_st);
+    if (h->h_oc) cudaFreeHost(h->h_oc);
+    if (h->h_scalar) cudaFreeHost(h->h_scalar);
+    if (h->own) cudaStreamDestroy(h->own);
+    delete h;
+    return TOG_OK;
+}
+
+int tog_set_stream(tog_handle* h, void* stream) {
+    TOG_TRY(check_handle(h));
+    TOG_CUDA(cudaStreamSynchronize(h->stream));
+    h->stream = stream ? (cudaStream_t)stream : h->own;
+    return TOG_OK;
+}
+
+int tog_set_fixed_dofs(tog_handle* h, int64_t n, const int32_t* dofs) {
+    TOG_TRY(check_handle(h));
+    if (n < 0 || (n > 0 && !dofs)) return fail(TOG_ERR_ARG, "bad fixed dof list");
+    std::vector<uint8_t> mask(h->nnodes, 0);
+    for (int64_t i = 0; i < n; ++i) {
+        const int32_t d = dofs[i];
+        if (d < 0 || d >= h->ndofs) return fail(TOG_ERR_ARG, "fixed dof out of range");
+        const int32_t k = h->ref2int[d];
+        mask[k / h->dim] |= (uint8_t)(1u << (k % h->dim));
+    }
+    TOG_CUDA(cudaMemcpyAsync(h->d_fixmask, mask.data(), h->nnodes, cudaMemcpyHostToDevice, h->stream));
+    TOG_CUDA(cudaStreamSynchronize(h->stream));
+    h->u_valid = false;
+    return TOG_OK;
+}
+
+int tog_set_rhs(tog_handle* h, const double* f) {
+    TOG_TRY(check_handle(h));
+    if (!f) return fail(TOG_ERR_ARG, "null rhs");
+    // masked copy: prescribed dofs carry no load (homogeneous Dirichlet, apply_zero!)
+    std::vector<uint8_t> mask(h->nnodes);
+    TOG_CUDA(cudaMemcpyAsync(mask.data(), h->d_fixmask, h->nnodes, cudaMemcpyDeviceToHost, h->stream));
+    TOG_CUDA(cudaStreamSynchronize(h->stream));
+    std::vector<double> fi(h->ndofs);
+    double s = 0;
+    for (long long i = 0; i < h->ndofs; ++i) {
+        const bool fixed = (mask[i / h->dim] >> (i % h->dim)) & 1u;
+        const double v = fixed ? 0.0 : f[h->node_dofs[i]];
+        if (!std::isfinite(v)) return fail(TOG_ERR_ARG, "rhs has non-finite entries");
+        fi[i] = v;
+        s += v * v;
+    }
+    h->fnorm2 = s;
+    TOG_CUDA(cudaMemcpyAsync(h->d_f, fi.data(), h->ndofs * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    TOG_CUDA(cudaStreamSynchronize(h->stream));
+    return TOG_OK;
+}
+
+int tog_set_penalty(tog_handle* h, double p) {
+    TOG_TRY(check_handle(h));
+    if (!(p >= 0) || !std::isfinite(p)) return fail(TOG_ERR_ARG, "penalty must be finite and >= 0");
+    h->p = p;
+    h->vars_dirty = true;
+    return TOG_OK;
+}
+
+int tog_set_vars(tog_handle* h, const double* x) {
+    TOG_TRY(check_handle(h));
+    if (!x) return fail(TOG_ERR_ARG, "null vars");
+    for (long long e = 0; e < h->ncells; ++e)
+        if (!std::isfinite(x[e])) return fail(TOG_ERR_ARG, "vars has non-finite entries");
+    TOG_CUDA(cudaMemcpyAsync(h->d_vars, x, h->ncells * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    h->vars_dirty = true;
+    return TOG_OK;
+}
+
+int tog_matvec(tog_handle* h, const double* x, double* y) {
+    TOG_TRY(check_handle(h));
+    if (!x || !y) return fail(TOG_ERR_ARG, "null vector");
+    TOG_TRY(refresh_scales(h));
+    TOG_TRY(upload_dofs(h, x, h->d_p64[0]));
+    launch_matvec<double, MV_PLAIN>(h, h->stream, h->d_p64[0], h->d_q64, nullptr);
+    TOG_CUDA(cudaGetLastError());
+    return download_dofs(h, h->d_q64, y);
+}
+
+int tog_solve(tog_handle* h, int32_t precision, double rtol, double abstol, int32_t maxiter, int32_t warm_start,
+              tog_solve_stats* stats) {
+    TOG_TRY(check_handle(h));
+    if (!(rtol >= 0) || !(abstol >= 0) || maxiter < 0) return fail(TOG_ERR_ARG, "bad tolerance or maxiter");
+    return do_solve(h, precision, rtol, abstol, maxiter, warm_start, stats);
+}
+
+int tog_get_u(tog_handle* h, double* u) {
+    TOG_TRY(check_handle(h));
+    if (!u) return fail(TOG_ERR_ARG, "null output");
+    return download_dofs(h, h->d_u, u);
+}
+
+int tog_set_u(tog_handle* h, const double* u) {
+    TOG_TRY(check_handle(h));
+    if (!u) return fail(TOG_ERR_ARG, "null input");
+    TOG_TRY(upload_dofs(h, u, h->d_u));
+    TOG_CUDA(cudaStreamSynchronize(h->stream));
+    h->u_valid = true;
+    return TOG_OK;
+}
+
+int tog_compliance(tog_handle* h, double* c, double* grad) {
+    TOG_TRY(check_handle(h));
+    if (!h->u_valid) return fail(TOG_ERR_STATE, "no displacement: call tog_solve first");
+    TOG_TRY(compliance_dev(h, h->d_grad));
+    if (grad)
+        TOG_CUDA(cudaMemcpyAsync(grad, h->d_grad, h->ncells * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    TOG_CUDA(cudaMemcpyAsync(h->h_scalar, h->d_scalar, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    TOG_CUDA(cudaStreamSynchronize(h->stream));
+    if (c) *c = h->h_scalar[0];
+    return TOG_OK;
+}
+
+int tog_filter_setup(tog_handle* h, double rmin) {
+    TOG_TRY(check_handle(h));
+    if (!(rmin > 0) || !std::isfinite(rmin)) return fail(TOG_ERR_ARG, "rmin must be > 0");
+    std::vector<int> off;
+    std::vector<double> w;
+    const int S = filter_stencil(h->dim, h->size, rmin, off, w);
+    if (S == 0)
+        return fail(TOG_ERR_ARG,
+                    "DensityFilterFun: no neighbouring nodes were found within the filter radius rmin for any "
+                    "element; rmin is likely smaller than the element size");
+    if (h->d_soff) cudaFree(h->d_soff);
+    if (h->d_sw) cudaFree(h->d_sw);
+    h->d_soff = nullptr;
+    h->d_sw = nullptr;
+    TOG_TRY(dalloc(&h->d_soff, off.size()));
+    TOG_TRY(dalloc(&h->d_sw, w.size()));
+    TOG_CUDA(cudaMemcpyAsync(h->d_soff, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+    TOG_CUDA(cudaMemcpyAsync(h->d_sw, w.data(), w.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    h->S = S;
+    if (h->dim == 3)
+        k_filt_invW<3><<<h->ew_blocks(h->ncells), kEwThreads, 0, h->stream>>>(h->d_soff, h->d_sw, S, h->d_invW,
+                                                                              h->dims());
+    else
+        k_filt_invW<2><<<h->ew_blocks(h->ncells), kEwThreads, 0, h->stream>>>(h->d_soff, h->d_sw, S, h->d_invW,
+                                                                              h->dims());
+    TOG_LAUNCHED(1);
+    TOG_CUDA(cudaGetLastError());
+    TOG_CUDA(cudaStreamSynchronize(h->stream));
+    h->filter_ready = true;
+    h->rmin = rmin;
+    return TOG_OK;
+}
+
+int tog_filter_apply(tog_handle* h, int32_t op, const double* in, double* out) {
+    TOG_TRY(check_handle(h));
+    if (!h->filter_ready) return fail(TOG_ERR_STATE, "tog_filter_setup has not been called");
+    if (!in || !out || (op != TOG_FILTER_J && op != TOG_FILTER_JT)) return fail(TOG_ERR_ARG, "bad filter arguments");
+    const size_t bytes = h->ncells * sizeof(double);
+    TOG_CUDA(cudaMemcpyAsync(h->d_xnew, in, bytes, cudaMemcpyHostToDevice, h->stream));
+    TOG_TRY(filter_dev(h, op, h->d_xnew, h->d_grad));
+    TOG_CUDA(cudaMemcpyAsync(out, h->d_grad, bytes, cudaMemcpyDeviceToHost, h->stream));
+    TOG_CUDA(cudaStreamSynchronize(h->stream));
+    return TOG_OK;
+}
+
+int tog_oc_update(tog_handle* h, const double* x, const double* dc, const double* dv, const double* vol_weights,
+                  double volfrac, double move, double* x_new, double* change, double* lambda) {
+    TOG_TRY(check_handle(h));
+    if (!x || !dc || !dv || !vol_weights || !x_new) return fail(TOG_ERR_ARG, "null array");
+    if (!(move > 0) || !(volfrac > 0 && volfrac <= 1)) return fail(TOG_ERR_ARG, "need move > 0 and 0 < volfrac <= 1");
+    if (h->simp_ready) return fail(TOG_ERR_STATE, "tog_oc_update shares buffers with an active tog_simp loop");
+    const size_t bytes = h->ncells * sizeof(double);
+    TOG_CUDA(cudaMemcpyAsync(h->d_x, x, bytes, cudaMemcpyHostToDevice, h->stream));
+    TOG_CUDA(cudaMemcpyAsync(h->d_dc, dc, bytes, cudaMemcpyHostToDevice, h->stream));
+    TOG_CUDA(cudaMemcpyAsync(h->d_dv, dv, bytes, cudaMemcpyHostToDevice, h->stream));
+    TOG_CUDA(cudaMemcpyAsync(h->d_w, vol_weights, bytes, cudaMemcpyHostToDevice, h->stream));
+    TOG_TRY(oc_dev(h, volfrac, move));
+    TOG_CUDA(cudaMemcpyAsync(x_new, h->d_xnew, bytes, cudaMemcpyDeviceToHost, h->stream));
+    TOG_CUDA(cudaStreamSynchronize(h->stream));
+    if (change) *change = h->h_oc->change;
+    if (lambda) *lambda = h->h_oc->lmid;
+    return TOG_OK;
+}
+
+int tog_simp_init(tog_handle* h, int32_t filter_kind, double rmin, double volfrac, double move, const double* x0) {
+    TOG_TRY(check_handle(h));
+    if (!x0) return fail(TOG_ERR_ARG, "null x0");
+    if (filter_kind < TOG_FILTER_NONE || filter_kind > TOG_FILTER_SENS) return fail(TOG_ERR_ARG, "bad filter kind");
+    if (!(move > 0) || !(volfrac > 0 && volfrac <= 1)) return fail(TOG_ERR_ARG, "need move > 0 and 0 < volfrac <= 1");
+    if (filter_kind != TOG_FILTER_NONE) TOG_TRY(tog_filter_setup(h, rmin));
+    h->simp_filter = filter_kind;
+    h->volfrac = volfrac;
+    h->move = move;
+    const size_t bytes = h->ncells * sizeof(double);
+    TOG_CUDA(cudaMemcpyAsync(h->d_x, x0, bytes, cudaMemcpyHostToDevice, h->stream));
+    // dv = d(volume fraction)/dx; for the density filter dv = J' (1/n) (volume.jl:59-67 + filter rrule),
+    // which is also the weight of x in the filtered volume used by the OC bisection.
+    std::vector<double> inv(h->ncells, 1.0 / (double)h->ncells);
+    TOG_CUDA(cudaMemcpyAsync(h->d_xnew, inv.data(), bytes, cudaMemcpyHostToDevice, h->stream));
+    if (filter_kind == TOG_FILTER_DENSITY) {
+        TOG_TRY(filter_dev(h, TOG_FILTER_JT, h->d_xnew, h->d_dv));
+    } else {
+        TOG_CUDA(cudaMemcpyAsync(h->d_dv, h->d_xnew, bytes, cudaMemcpyDeviceToDevice, h->stream));
+    }
+    TOG_CUDA(cudaMemcpyAsync(h->d_w, h->d_dv, bytes, cudaMemcpyDeviceToDevice, h->stream));
+    TOG_CUDA(cudaStreamSynchronize(h->stream));
+    h->simp_ready = true;
+    h->u_valid = false;
+    return TOG_OK;
+}
+
+int tog_simp_step(tog_handle* h, int32_t precision, double rtol, int32_t maxiter, int32_t warm_start,
+                  tog_iter_stats* stats) {
+    TOG_TRY(check_handle(h));
+    if (!h->simp_ready) return fail(TOG_ERR_STATE, "tog_simp_init has not been called");
+    const size_t bytes = h->ncells * sizeof(double);
+    // physical densities
+    if (h->simp_filter == TOG_FILTER_DENSITY)
+        TOG_TRY(filter_dev(h, TOG_FILTER_J, h->d_x, h->d_vars));
+    else
+        TOG_CUDA(cudaMemcpyAsync(h->d_vars, h->d_x, bytes, cudaMemcpyDeviceToDevice, h->stream));
+    h->vars_dirty = true;
+    tog_solve_stats ss{};
+    int rc = do_solve(h, precision, rtol, 0.0, maxiter, warm_start, &ss);
+    if (rc != TOG_OK && rc != TOG_NOT_CONVERGED) return rc;
+    TOG_TRY(compliance_dev(h, h->d_grad));
+    if (h->simp_filter == TOG_FILTER_DENSITY)
+        TOG_TRY(filter_dev(h, TOG_FILTER_JT, h->d_grad, h->d_dc));
+    else if (h->simp_filter == TOG_FILTER_SENS)
+        TOG_TRY(filter_dev(h, TOG_FILTER_J, h->d_grad, h->d_dc));
+    else
+        TOG_CUDA(cudaMemcpyAsync(h->d_dc, h->d_grad, bytes, cudaMemcpyDeviceToDevice, h->stream));
+    TOG_TRY(oc_dev(h, h->volfrac, h->move));
+    TOG_CUDA(cudaMemcpyAsync(h->h_scalar, h->d_scalar, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    TOG_CUDA(cudaStreamSynchronize(h->stream));
+    TOG_CUDA(cudaMemcpyAsync(h->d_x, h->d_xnew, bytes, cudaMemcpyDeviceToDevice, h->stream));
+    TOG_CUDA(cudaStreamSynchronize(h->stream));
+    if (stats) {
+        stats->compliance = h->h_scalar[0];
+        stats->volume = h->h_oc->vol;
+        stats->change = h->h_oc->change;
+        stats->lambda = h->h_oc->lmid;
+        stats->cg_iterations = ss.iterations;
+        stats->outer_iterations = ss.outer_iterations;
+        stats->oc_steps = h->h_oc->steps;
+        stats->status = ss.status;
+        stats->rel_residual = ss.rel_residual;
+    }
+    return rc;
+}
+
+int tog_get_design(tog_handle* h, double* x) {
+    TOG_TRY(check_handle(h));
+    if (!x) return fail(TOG_ERR_ARG, "null output");
+    TOG_CUDA(cudaMemcpyAsync(x, h->d_x, h->ncells * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    TOG_CUDA(cudaStreamSynchronize(h->stream));
+    return TOG_OK;
+}
+
+int tog_set_design(tog_handle* h, const double* x) {
+    TOG_TRY(check_handle(h));
+    if (!x) return fail(TOG_ERR_ARG, "null input");
+    TOG_CUDA(cudaMemcpyAsync(h->d_x, x, h->ncells * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    return TOG_OK;
+}
+
+int tog_get_physical(tog_handle* h, double* xf) {
+    TOG_TRY(check_handle(h));
+    if (!xf) return fail(TOG_ERR_ARG, "null output");
+    TOG_CUDA(cudaMemcpyAsync(xf, h->d_vars, h->ncells * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    TOG_CUDA(cudaStreamSynchronize(h->stream));
+    return TOG_OK;
+}
+
+int tog_bench_pcg_matvec(tog_handle* h, int32_t precision, int32_t nlaunch) {
+    TOG_TRY(check_handle(h));
+    if (nlaunch < 0) return fail(TOG_ERR_ARG, "nlaunch < 0");
+    TOG_TRY(refresh_scales(h));
+    if (h->fnorm2 <= 0) return fail(TOG_ERR_STATE, "set a non-zero rhs first");
+    if (precision == TOG_FP64) {
+        TOG_CUDA(cudaMemcpyAsync(h->d_r64, h->d_f, h->ndofs * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+        launch_pcg_init<double>(h, h->stream, 0, 0.0, 0.0, h->fnorm2, 1 << 30);
+        for (int i = 0; i < nlaunch; ++i) launch_matvec<double, MV_PCG>(h, h->stream, nullptr, nullptr, nullptr);
+    } else {
+        TOG_CUDA(cudaMemcpyAsync(h->d_r64, h->d_f, h->ndofs * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+        TOG_CUDA(cudaMemcpyAsync(&h->d_st64->rr, &h->fnorm2, sizeof(double), cudaMemcpyHostToDevice, h->stream));
+        TOG_CUDA(cudaStreamSynchronize(h->stream));
+        const int nb = h->ew_blocks(h->ndofs);
+        if (h->dim == 3)
+            k_ir_scale<3><<<nb, kEwThreads, 0, h->stream>>>(h->d_r64, h->d_r32, h->ndofs, h->d_st64);
+        else
+            k_ir_scale<2><<<nb, kEwThreads, 0, h->stream>>>(h->d_r64, h->d_r32, h->ndofs, h->d_st64);
+        TOG_LAUNCHED(1);
+        launch_pcg_init<float>(h, h->stream, 1, 0.0, 0.0, -1.0, 1 << 30);
+        for (int i = 0; i < nlaunch; ++i) launch_matvec<float, MV_PCG>(h, h->stream, nullptr, nullptr, nullptr);
+    }
+    TOG_CUDA(cudaGetLastError());
+    return TOG_OK;
+}
+
+int tog_pcg_matvec_bytes(tog_handle* h, int32_t precision, double* bytes) {
+    TOG_TRY(check_handle(h));
+    if (!bytes) return fail(TOG_ERR_ARG, "null output");
+    const double s = precision == TOG_FP64 ? 8.0 : 4.0;
+    // reads r, p_old (N each), dinv (per node), E_e (per cell), fixmask (1 B per node);
+    // writes p, q (N each)
+    *bytes = 4.0 * s * (double)h->ndofs + s * (double)h->nnodes + s * (double)h->ncells + (double)h->nnodes;
+    return TOG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,367 @@
+"""Host-side mirror of TopOpt.jl's API for the SIMP compliance path, driving
+libtopopt_gb300 through its C ABI.  Names, argument meanings, defaults and
+error behaviour follow the reference (paths relative to the TopOpt.jl root):
+
+  PointLoadCantilever, HalfMBB      src/TopOptProblems/problem_types.jl:162-231, 324-395
+  FEASolver(GB300Solver, problem)   src/FEA/solvers_api.jl:468-603 (CGMatrixFreeSolver's slot)
+  PowerPenaltyFun                   src/Utilities/penalties.jl:30-33
+  PseudoDensities                   src/TopOpt.jl:30-74
+  ComplianceFun (+ pullback)        src/Functions/compliance.jl:28-76
+  VolumeFun (+ pullback)            src/Functions/volume.jl:47-67
+  DensityFilterFun / SensFilterFun  src/CheqFilters/density_filter.jl:25-47, sens_filter.jl:29-111
+  oc_update, SIMPLoop               published OC update (no reference counterpart)
+"""
+import math
+
+import numpy as np
+
+from . import _lib as L
+
+
+# --------------------------------------------------------------------------- numbering
+def grid_counts(nels):
+    nel = (L.C.c_int32 * 3)(*(list(nels) + [1] * (3 - len(nels))))
+    nn, nc, nd = L.C.c_int64(), L.C.c_int64(), L.C.c_int64()
+    L.check(L.lib().tog_grid_counts(len(nels), nel, L.C.byref(nn), L.C.byref(nc), L.C.byref(nd)))
+    return nn.value, nc.value, nd.value
+
+
+def node_dofs(nels):
+    """Metadata.node_dofs as a (nnodes, dim) array of 0-based dofs (metadata.jl:116-145)."""
+    dim = len(nels)
+    nn, _, _ = grid_counts(nels)
+    out = np.empty(nn * dim, dtype=np.int32)
+    nel = (L.C.c_int32 * 3)(*(list(nels) + [1] * (3 - dim)))
+    L.check(L.lib().tog_node_dofs(dim, nel, L.iptr(out)))
+    return out.reshape(nn, dim)
+
+
+def cell_dofs(nels):
+    """Metadata.cell_dofs as a (ncells, ndpc) array of 0-based dofs (metadata.jl:40-50)."""
+    dim = len(nels)
+    _, nc, _ = grid_counts(nels)
+    ndpc = (2 ** dim) * dim
+    out = np.empty(nc * ndpc, dtype=np.int32)
+    nel = (L.C.c_int32 * 3)(*(list(nels) + [1] * (3 - dim)))
+    L.check(L.lib().tog_cell_dofs(dim, nel, L.iptr(out)))
+    return out.reshape(nc, ndpc)
+
+
+def element_stiffness(dim, sizes, E, nu, plane_stress=False):
+    nd = (2 ** dim) * dim
+    Ke = np.empty(nd * nd)
+    sz = (L.C.c_double * 3)(*(list(sizes) + [1.0] * (3 - dim)))
+    L.check(L.lib().tog_element_stiffness(dim, sz, E, nu, int(plane_stress), L.dptr(Ke)))
+    return Ke.reshape(nd, nd)
+
+
+# --------------------------------------------------------------------------- problems
+class _StructuredProblem:
+    def __init__(self, nels, sizes, E, nu, force, plane_stress):
+        self.nels = tuple(int(n) for n in nels)
+        self.sizes = tuple(float(s) for s in sizes)
+        self.dim = len(self.nels)
+        if self.dim not in (2, 3) or len(self.sizes) != self.dim:
+            raise ValueError("nels and sizes must both have 2 or 3 entries")
+        self.E, self.nu, self.force = float(E), float(nu), float(force)
+        self.plane_stress = bool(plane_stress)
+        self.nnodes, self.ncells, self.ndofs = grid_counts(self.nels)
+        self.node_dofs = node_dofs(self.nels)          # (nnodes, dim)
+        self.nn = tuple(n + 1 for n in self.nels)
+
+    def node_id(self, ix, iy, iz=0):
+        return ix + self.nn[0] * (iy + self.nn[1] * iz)
+
+    def _node_grid(self):
+        idx = np.arange(self.nnodes)
+        ix = idx % self.nn[0]
+        iy = (idx // self.nn[0]) % self.nn[1]
+        iz = idx // (self.nn[0] * self.nn[1]) if self.dim == 3 else np.zeros_like(idx)
+        return ix, iy, iz
+
+    def load_vector(self):
+        f = np.zeros(self.ndofs)
+        f[self.force_dof] = -self.force     # getcloaddict: [0, -force, 0] (problem_types.jl:398-402)
+        return f
+
+
+class PointLoadCantilever(_StructuredProblem):
+    """Left face clamped; load [0, -force, 0] at the first node of right & middley
+    (problem_types.jl:162-231).  load='face_centre' moves the 3D load to the
+    centre of the right face (not the reference's node)."""
+
+    def __init__(self, nels, sizes, E=1.0, nu=0.3, force=1.0, *, load="reference_first_node",
+                 plane_stress=False):
+        if nels[1] % 2 or (len(nels) == 3 and nels[2] % 2):
+            raise ValueError("Grid does not have an even number of elements along the y and/or z axes.")
+        super().__init__(nels, sizes, E, nu, force, plane_stress)
+        ix, iy, iz = self._node_grid()
+        left = np.nonzero(ix == 0)[0]
+        self.fixed_dofs = np.sort(self.node_dofs[left].ravel()).astype(np.int32)
+        kz = self.nels[2] // 2 if (self.dim == 3 and load == "face_centre") else 0
+        self.load_node = self.node_id(self.nels[0], self.nels[1] // 2, kz)
+        self.force_dof = int(self.node_dofs[self.load_node, 1])
+
+
+class HalfMBB(_StructuredProblem):
+    """u1 = 0 on the left face, u2 = 0 on bottom & right, load [0, -force] at the
+    first node of top & left (problem_types.jl:324-395)."""
+
+    def __init__(self, nels, sizes, E=1.0, nu=0.3, force=1.0, *, plane_stress=False):
+        super().__init__(nels, sizes, E, nu, force, plane_stress)
+        ix, iy, iz = self._node_grid()
+        f1 = self.node_dofs[np.nonzero(ix == 0)[0], 0]
+        f2 = self.node_dofs[np.nonzero((iy == 0) & (ix == self.nels[0]))[0], 1]
+        self.fixed_dofs = np.sort(np.concatenate([f1, f2])).astype(np.int32)
+        self.load_node = self.node_id(0, self.nels[1], 0)
+        self.force_dof = int(self.node_dofs[self.load_node, 1])
+
+
+# --------------------------------------------------------------------------- solver
+class PowerPenaltyFun:
+    def __init__(self, p):
+        self.p = float(p)
+
+
+class PseudoDensities:
+    def __init__(self, x):
+        self.x = np.ascontiguousarray(x, dtype=np.float64)
+
+
+class GB300Solver:
+    """Marker type: FEASolver(GB300Solver, problem; ...) -- the AbstractLinearSolver
+    slot of solvers_api.jl:44 filled by libtopopt_gb300."""
+
+
+PRECISIONS = {"fp64": L.TOG_FP64, "fp32_ir": L.TOG_FP32_IR}
+
+
+class GB300FEASolver:
+    """Matrix-free SIMP solver resident on the GPU.  Defaults follow
+    FEASolver (solvers_api.jl:468-489): xmin = 1e-3, penalty = PowerPenaltyFun(1),
+    cg_max_iter = 700, abstol = 1e-7, rtol = sqrt(eps) (IterativeSolvers' reltol)."""
+
+    def __init__(self, problem, *, xmin=None, penalty=None, cg_max_iter=700, abstol=None, rtol=None,
+                 precision="fp64", warm_start=False):
+        self.problem = problem
+        self.xmin = 1e-3 if xmin is None else float(xmin)
+        self.penalty = PowerPenaltyFun(1.0) if penalty is None else penalty
+        self.cg_max_iter = int(cg_max_iter)
+        self.abstol = 1e-7 if abstol is None else float(abstol)
+        self.rtol = math.sqrt(np.finfo(np.float64).eps) if rtol is None else float(rtol)
+        if precision not in PRECISIONS:
+            raise ValueError("precision must be one of %s" % sorted(PRECISIONS))
+        self.precision = precision
+        self.warm_start = bool(warm_start)
+        d = L.ProblemDesc()
+        d.dim = problem.dim
+        for i in range(problem.dim):
+            d.nel[i] = problem.nels[i]
+            d.size[i] = problem.sizes[i]
+        d.E, d.nu, d.plane_stress = problem.E, problem.nu, int(problem.plane_stress)
+        d.xmin, d.penalty = self.xmin, self.penalty.p
+        h = L.C.c_void_p()
+        L.check(L.lib().tog_create(L.C.byref(d), L.C.byref(h)))
+        self.handle = h
+        fd = np.ascontiguousarray(problem.fixed_dofs, dtype=np.int32)
+        L.check(L.lib().tog_set_fixed_dofs(h, len(fd), L.iptr(fd)))
+        f = np.ascontiguousarray(problem.load_vector())
+        L.check(L.lib().tog_set_rhs(h, L.dptr(f)))
+        self.vars = np.ones(problem.ncells)          # solvers_api.jl:502
+        self.last_stats = None
+
+    # -- reference-style accessors
+    def close(self):
+        if getattr(self, "handle", None):
+            L.lib().tog_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def setpenalty(self, p):
+        self.penalty = p if isinstance(p, PowerPenaltyFun) else PowerPenaltyFun(p)
+        L.check(L.lib().tog_set_penalty(self.handle, self.penalty.p))
+
+    def _push_vars(self):
+        v = np.ascontiguousarray(self.vars, dtype=np.float64)
+        if v.shape != (self.problem.ncells,):
+            raise ValueError("DimensionMismatch: vars must have one entry per cell")
+        L.check(L.lib().tog_set_vars(self.handle, L.dptr(v)))
+
+    def __call__(self, precision=None, warm_start=None):
+        """solver(): solve K(vars) u = f (solvers_api.jl:285-374)."""
+        self._push_vars()
+        st = L.SolveStats()
+        prec = PRECISIONS[precision or self.precision]
+        warm = self.warm_start if warm_start is None else warm_start
+        L.check(L.lib().tog_solve(self.handle, prec, self.rtol, self.abstol, self.cg_max_iter, int(warm),
+                                  L.C.byref(st)))
+        self.last_stats = st
+        return None
+
+    @property
+    def u(self):
+        out = np.empty(self.problem.ndofs)
+        L.check(L.lib().tog_get_u(self.handle, L.dptr(out)))
+        return out
+
+    @u.setter
+    def u(self, v):
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        L.check(L.lib().tog_set_u(self.handle, L.dptr(v)))
+
+    def matvec(self, x):
+        """mul!(y, MatrixFreeOperator, x) at the current vars (matrix_free_operator.jl:66-105)."""
+        self._push_vars()
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.empty_like(x)
+        L.check(L.lib().tog_matvec(self.handle, L.dptr(x), L.dptr(y)))
+        return y
+
+
+def FEASolver(solver_type, problem, **kw):
+    if solver_type is not GB300Solver:
+        raise ValueError("this library provides FEASolver(GB300Solver, problem; ...)")
+    return GB300FEASolver(problem, **kw)
+
+
+# --------------------------------------------------------------------------- functions
+class ComplianceFun:
+    """J = sum rho_e u_e' Ke u_e with dJ/dx_e = -drho_e u_e' Ke u_e (compliance.jl:58-76)."""
+
+    def __init__(self, solver):
+        self.solver = solver
+        self.grad = np.zeros(solver.problem.ncells)
+        self.cell_comp = None
+
+    def __call__(self, x):
+        if not isinstance(x, PseudoDensities):
+            x = PseudoDensities(x)
+        s = self.solver
+        s.vars = x.x.copy()
+        s()
+        c = L.C.c_double()
+        g = np.empty(s.problem.ncells)
+        L.check(L.lib().tog_compliance(s.handle, L.C.byref(c), L.dptr(g)))
+        self.grad = g
+        return c.value
+
+    def pullback(self, delta=1.0):
+        return self.grad * delta
+
+
+class VolumeFun:
+    """Volume fraction sum x_e v_e / sum v_e and its constant gradient (volume.jl:47-67)."""
+
+    def __init__(self, solver, fraction=True):
+        n = solver.problem.ncells
+        self.cellvolumes = np.full(n, float(np.prod(solver.problem.sizes)))
+        self.total_volume = float(self.cellvolumes.sum())
+        self.fraction = fraction
+        self.grad = self.cellvolumes / self.total_volume if fraction else self.cellvolumes.copy()
+
+    def __call__(self, x):
+        x = x.x if isinstance(x, PseudoDensities) else np.asarray(x)
+        v = float(np.dot(self.cellvolumes, x))
+        return v / self.total_volume if self.fraction else v
+
+    def pullback(self, delta=1.0):
+        return self.grad * delta
+
+
+class _NodeFilter:
+    def __init__(self, solver, rmin):
+        self.solver = solver
+        self.rmin = float(rmin)
+        try:
+            L.check(L.lib().tog_filter_setup(solver.handle, self.rmin))
+        except L.TopOptError as e:
+            if e.code == L.TOG_ERR_ARG:
+                raise ValueError(str(e)) from None   # ArgumentError in the reference
+            raise
+
+    def _apply(self, op, v):
+        v = np.ascontiguousarray(v.x if isinstance(v, PseudoDensities) else v, dtype=np.float64)
+        out = np.empty_like(v)
+        L.check(L.lib().tog_filter_apply(self.solver.handle, op, L.dptr(v), L.dptr(out)))
+        return out
+
+
+class DensityFilterFun(_NodeFilter):
+    """y = J x; pullback J' * delta (density_filter.jl:35-47)."""
+
+    def __call__(self, x):
+        return PseudoDensities(self._apply(L.TOG_FILTER_J, x))
+
+    def pullback(self, delta):
+        return self._apply(L.TOG_FILTER_JT, delta)
+
+
+class SensFilterFun(_NodeFilter):
+    """Identity forward; pullback applies the node and cone averages, J * delta
+    (sens_filter.jl:49-111)."""
+
+    def __call__(self, x):
+        return PseudoDensities(np.array(x.x if isinstance(x, PseudoDensities) else x, dtype=np.float64))
+
+    def pullback(self, delta):
+        return self._apply(L.TOG_FILTER_J, delta)
+
+
+def oc_update(solver, x, dc, dv, vol_weights, volfrac, move=0.2):
+    """Optimality-criteria update (published method; no reference counterpart).
+    Returns (x_new, change, lambda)."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    dc = np.ascontiguousarray(dc, dtype=np.float64)
+    dv = np.ascontiguousarray(dv, dtype=np.float64)
+    w = np.ascontiguousarray(vol_weights, dtype=np.float64)
+    xn = np.empty_like(x)
+    ch, lam = L.C.c_double(), L.C.c_double()
+    L.check(L.lib().tog_oc_update(solver.handle, L.dptr(x), L.dptr(dc), L.dptr(dv), L.dptr(w), float(volfrac),
+                                  float(move), L.dptr(xn), L.C.byref(ch), L.C.byref(lam)))
+    return xn, ch.value, lam.value
+
+
+class SIMPLoop:
+    """Device-resident SIMP design loop: filter -> solve -> compliance/sensitivities
+    -> filter pullback -> OC, one C-ABI call per design iteration."""
+
+    FILTERS = {"none": L.TOG_FILTER_NONE, "density": L.TOG_FILTER_DENSITY, "sens": L.TOG_FILTER_SENS}
+
+    def __init__(self, solver, *, volfrac, rmin=0.0, filter="density", move=0.2, x0=None):
+        self.solver = solver
+        n = solver.problem.ncells
+        x0 = np.full(n, float(volfrac)) if x0 is None else np.ascontiguousarray(x0, dtype=np.float64)
+        L.check(L.lib().tog_simp_init(solver.handle, self.FILTERS[filter], float(rmin), float(volfrac), float(move),
+                                      L.dptr(x0)))
+
+    def step(self, precision=None, rtol=None, maxiter=None, warm_start=None):
+        s = self.solver
+        st = L.IterStats()
+        code = L.lib().tog_simp_step(s.handle, PRECISIONS[precision or s.precision],
+                                     s.rtol if rtol is None else float(rtol),
+                                     s.cg_max_iter if maxiter is None else int(maxiter),
+                                     int(s.warm_start if warm_start is None else warm_start), L.C.byref(st))
+        L.check(code)
+        return st
+
+    @property
+    def x(self):
+        out = np.empty(self.solver.problem.ncells)
+        L.check(L.lib().tog_get_design(self.solver.handle, L.dptr(out)))
+        return out
+
+    @x.setter
+    def x(self, v):
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        L.check(L.lib().tog_set_design(self.solver.handle, L.dptr(v)))
+
+    @property
+    def physical(self):
+        out = np.empty(self.solver.problem.ncells)
+        L.check(L.lib().tog_get_physical(self.solver.handle, L.dptr(out)))
+        return out
