@@ -1,0 +1,354 @@
+"""Benchmark: SIMP design iterations/s on a 3D hex8 cantilever (160x80x80,
+1,024,000 elements), one GB300.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+A step is one design iteration (density filter -> solve to rtol 1e-8 ->
+compliance + sensitivities -> filter pullback -> OC update), timed with CUDA
+events on the stream the library launches on.  `value` is the device-resident
+loop; `e2e` is the same loop through the C ABI with the design copied from and
+to pinned host memory every step.  N > 1 runs independent replicas (the path
+does not shard: one problem per GPU).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "design iters/s, 3D hex8 1M elems: learned+FP32-IR vs plain FP64 PCG @ rel 1e-6"
+NELS = (160, 80, 80)
+VOLFRAC, RMIN, PEN, XMIN, RTOL, MOVE = 0.3, 1.5, 3.0, 1e-9, 1e-8, 0.2
+WORKLOAD = ("3D PointLoadCantilever 160x80x80 hex8 (1,024,000 elements, 3,168,963 dofs), E0=1, nu=0.3, "
+            "E_min=1e-9, unit load at the right-face centre, SIMP p=3, V=0.3, density filter rmin=1.5, "
+            "x0=0.3, OC move 0.2, solve rtol 1e-8")
+# FP64 Jacobi-PCG iterations per design iteration on this workload (cold start,
+# rtol 1e-8), measured by this script's FP64 leg on a GB300; the CPU reference
+# arm multiplies its measured per-iteration time by it.
+REF_CG_ITERS_DEFAULT = 1000
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def read_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def read_traffic():
+    """dram bytes per launch of the PCG operator kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "k_matvec3_fp32_pcg_160x80x80.md")
+    try:
+        for line in open(p):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":")[1])
+    except Exception:
+        pass
+    return None
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.rows = []
+        if self.proc:
+            self.proc.terminate()
+            out, _ = self.proc.communicate(timeout=10)
+            for line in out.strip().splitlines():
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    self.rows.append(parts)
+
+    def summary(self):
+        if not getattr(self, "rows", None):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def max_over_ranks(v, ws):
+    if ws == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+# --------------------------------------------------------------------------- CPU legs
+def cpu_sample(threads, cg_iters, sample_iters):
+    """Time the oracle port of the reference path on the host: one full set of the
+    non-solve work (filter, compliance, filter pullback, OC) plus `sample_iters`
+    Jacobi-PCG iterations; scale the PCG part to `cg_iters` iterations per design
+    iteration."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import topopt_oracle as O
+    import oracle_cpu as OC
+    prob = O.point_load_cantilever(NELS, (1.0, 1.0, 1.0), load="face_centre")
+    Ke = O.element_stiffness(3, (1.0, 1.0, 1.0), 1.0, 0.3)
+    t0 = time.perf_counter()
+    cs = OC.CPUSolver(prob, Ke, XMIN, PEN, threads=threads)
+    t_setup = time.perf_counter() - t0
+    n = prob.grid.ncells
+    x = np.full(n, VOLFRAC)
+    cs.filter_setup(RMIN)
+    t0 = time.perf_counter()
+    xf = cs.filter_J(x)
+    cs.set_vars(xf)
+    t_a = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    u, it, _ = cs.pcg(prob.f, rtol=0.0, abstol=0.0, maxit=sample_iters)
+    t_pcg = (time.perf_counter() - t0) / max(it, 1)
+    t0 = time.perf_counter()
+    c, g = cs.compliance(u)
+    dc = cs.filter_JT(g)
+    dv = cs.filter_JT(np.full(n, 1.0 / n))
+    cs.oc(x, dc, dv, dv, VOLFRAC, MOVE)
+    t_b = time.perf_counter() - t0
+    cs.close()
+    per_iter = t_a + t_b + cg_iters * t_pcg
+    return dict(seconds_per_design_iter=per_iter, seconds_per_pcg_iter=t_pcg, other_seconds=t_a + t_b,
+                setup_seconds=t_setup, sample_pcg_iters=it)
+
+
+def run_reference(args):
+    ws, rank, _ = dist_setup()
+    if rank != 0:
+        return 0
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_cpu as OC
+    threads = OC.lib().orc_max_threads()
+    cg_iters = int(os.environ.get("REF_CG_ITERS", REF_CG_ITERS_DEFAULT))
+    per = []
+    for s in range(args.warmup + args.steps):
+        r = cpu_sample(threads, cg_iters, sample_iters=3)
+        if s >= args.warmup:
+            per.append(r["seconds_per_design_iter"])
+    v = len(per) / sum(per)
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "design_iters/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(per) / len(per),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD},
+            "cpu_baseline": {"value": v, "unit": "design_iters/s", "cores": threads, "kind": "port",
+                             "sample": "per step: filter + compliance + filter pullback + OC once, 3 Jacobi-PCG "
+                                       "iterations timed and scaled to %d iterations per design iteration "
+                                       "(the FP64 PCG count of this workload)" % cg_iters},
+            "e2e": {"value": v, "unit": "design_iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# --------------------------------------------------------------------------- GPU leg
+def run_ours(args):
+    import torch
+    ws, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import __graft_entry__ as ge
+    tg = ge.load()
+    L = tg._lib
+    stream = torch.cuda.Stream()
+    prob = tg.PointLoadCantilever(NELS, (1.0, 1.0, 1.0), load="face_centre")
+    n = prob.ncells
+
+    def make_solver(precision, warm):
+        s = tg.FEASolver(tg.GB300Solver, prob, xmin=XMIN, penalty=tg.PowerPenaltyFun(PEN), rtol=RTOL, abstol=0.0,
+                         cg_max_iter=200000, precision=precision, warm_start=warm)
+        L.check(L.lib().tog_set_stream(s.handle, L.C.c_void_p(stream.cuda_stream)))
+        return s
+
+    # ---- optimised path: FP32 K*u / PCG inside FP64 refinement, warm start from the previous step
+    solver = make_solver("fp32_ir", True)
+    loop = tg.SIMPLoop(solver, volfrac=VOLFRAC, rmin=RMIN, filter="density")
+    stats = []
+    for _ in range(args.warmup):
+        loop.step()
+    torch.cuda.synchronize()
+    barrier(ws)
+    l0 = L.lib().tog_launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            for _ in range(args.steps):
+                stats.append(loop.step())
+            e1.record(stream)
+        torch.cuda.synchronize()
+    launches = L.lib().tog_launch_count() - l0
+    t_dev = e0.elapsed_time(e1) / 1e3
+    t_dev = max_over_ranks(t_dev, ws)
+    value = ws * args.steps / t_dev
+    clocks = clk.summary()
+
+    # ---- e2e: same loop through the C ABI with the design in pinned host memory
+    xh = torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
+    xh[:] = loop.x
+    e_steps = max(2, min(args.steps, 5))
+    torch.cuda.synchronize()
+    barrier(ws)
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        f0.record(stream)
+        for _ in range(e_steps):
+            L.check(L.lib().tog_set_design(solver.handle, L.dptr(xh)))
+            st = L.IterStats()
+            L.check(L.lib().tog_simp_step(solver.handle, L.TOG_FP32_IR, RTOL, 200000, 1, L.C.byref(st)))
+            L.check(L.lib().tog_get_design(solver.handle, L.dptr(xh)))
+        f1.record(stream)
+    torch.cuda.synchronize()
+    t_e2e = max_over_ranks(f0.elapsed_time(f1) / 1e3, ws)
+    e2e = {"value": ws * e_steps / t_e2e, "unit": "design_iters/s", "h2d_bytes_per_step": 8 * n,
+           "d2h_bytes_per_step": 8 * n + 8}
+
+    # ---- accuracy: FP32-IR vs FP64 PCG on the same filtered design
+    xphys = loop.physical
+    acc = {}
+    s64 = make_solver("fp64", False)
+    comp64 = tg.ComplianceFun(s64)
+    c64 = comp64(tg.PseudoDensities(xphys))
+    it64 = s64.last_stats.iterations
+    comp32 = tg.ComplianceFun(solver)
+    solver.warm_start = False
+    c32 = comp32(tg.PseudoDensities(xphys))
+    solver.warm_start = True
+    acc = {"compliance_rel_err": abs(c32 - c64) / abs(c64),
+           "sens_rel_err": float(np.max(np.abs(comp32.grad - comp64.grad)) / np.max(np.abs(comp64.grad))),
+           "fp64_cg_iters": it64, "fp32ir_inner_iters_cold": solver.last_stats.iterations,
+           "fp32ir_outer_iters_cold": solver.last_stats.outer_iterations}
+
+    # ---- plain FP64 Jacobi PCG design iterations (cold start, as the reference)
+    loop64 = tg.SIMPLoop(s64, volfrac=VOLFRAC, rmin=RMIN, filter="density")
+    k64 = max(1, min(args.steps, int(os.environ.get("FP64_STEPS", "2"))))
+    loop64.step(precision="fp64", warm_start=False)   # warm-up
+    g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    st64 = []
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        g0.record(stream)
+        for _ in range(k64):
+            st64.append(loop64.step(precision="fp64", warm_start=False))
+        g1.record(stream)
+    torch.cuda.synchronize()
+    t64 = g0.elapsed_time(g1) / 1e3
+    fp64 = {"value": k64 / t64, "unit": "design_iters/s", "steps": k64,
+            "cg_iters_per_step": [int(s.cg_iterations) for s in st64]}
+    s64.close()
+
+    # ---- roofline of the dominant kernel: FP32 PCG operator (k_matvec3<float, PCG>)
+    nl = 200
+    L.check(L.lib().tog_bench_pcg_matvec(solver.handle, L.TOG_FP32_IR, 10))
+    torch.cuda.synchronize()
+    h0, h1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        h0.record(stream)
+        L.check(L.lib().tog_bench_pcg_matvec(solver.handle, L.TOG_FP32_IR, nl))
+        h1.record(stream)
+    torch.cuda.synchronize()
+    t_k = h0.elapsed_time(h1) / 1e3 / nl
+    nbytes = L.C.c_double()
+    L.check(L.lib().tog_pcg_matvec_bytes(solver.handle, L.TOG_FP32_IR, L.C.byref(nbytes)))
+    peaks, src = read_peaks()
+    achieved = nbytes.value / t_k / 1e9
+    roof = {"bound": "hbm", "kernel": "k_matvec3<float, PCG>", "achieved": achieved, "peak": peaks["hbm_gbs"],
+            "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": read_traffic(),
+            "algorithmic_bytes_per_launch": nbytes.value, "us_per_launch": t_k * 1e6,
+            "peak_source": src + " (MEASURED_PEAKS.json hbm_gbs, burst copy)" if src == "measured" else src}
+    solver.close()
+
+    cg = [int(s.cg_iterations) for s in stats]
+    line = {"metric": METRIC, "value": value, "unit": "design_iters/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 K*u and PCG inside f64 refinement",
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD, "method": "FP32-IR + previous-step warm start",
+                       "l2": "working set ~0.3 GB per GPU > 129 MB L2 (no flush)",
+                       "parallelism": "replicas" if ws > 1 else "single GPU"},
+            "clocks": clocks, "e2e": e2e, "gpu_launches": int(launches), "roofline": roof,
+            "fp64_pcg": fp64, "accuracy_vs_fp64": acc,
+            "inner_cg_iters_per_step": cg,
+            "outer_iters_per_step": [int(s.outer_iterations) for s in stats],
+            "compliance_last": stats[-1].compliance}
+    if rank == 0 and not args.no_cpu:
+        os.environ.setdefault("OMP_NUM_THREADS", "1")
+        r = cpu_sample(1, it64, sample_iters=3)
+        line["cpu_baseline"] = {"value": 1.0 / r["seconds_per_design_iter"], "unit": "design_iters/s", "cores": 1,
+                                "kind": "port",
+                                "sample": "oracle port of the reference matrix-free path (per-element Ke, two-phase "
+                                          "gather): filter + compliance + pullback + OC once, 3 Jacobi-PCG iterations "
+                                          "timed and scaled to %d iterations (the FP64 PCG count at the first design "
+                                          "iteration)" % it64,
+                                "seconds_per_pcg_iter": r["seconds_per_pcg_iter"]}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        log("warmup raised to 3 (timing rule)")
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

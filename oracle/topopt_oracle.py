@@ -74,28 +74,21 @@ def rectilinear_grid(nels, sizes) -> Grid:
     (grids.jl:66-92; pinned in 2D by test/topopt_problems/metadata.jl:53-77)."""
     dim = len(nels)
     nn = [n + 1 for n in nels]
-    axes = [np.arange(nn[d], dtype=np.float64) * (nels[d] * sizes[d]) / nels[d]
-            for d in range(dim)]
     # Ferrite generate_grid places nodes by linear interpolation between the corners.
+    axes = [np.arange(nn[d], dtype=np.float64) * (nels[d] * sizes[d]) / nels[d] for d in range(dim)]
     if dim == 2:
-        X, Y = np.meshgrid(axes[0], axes[1], indexing="xy")
+        Y, X = np.meshgrid(axes[1], axes[0], indexing="ij")
         coords = np.stack([X.ravel(), Y.ravel()], axis=1)
-        nid = lambda i, j: i + nn[0] * j
-        cells = []
-        for j in range(nels[1]):
-            for i in range(nels[0]):
-                cells.append([nid(i + a, j + b) for (a, b) in QUAD_CORNERS])
+        J, I = np.meshgrid(np.arange(nels[1]), np.arange(nels[0]), indexing="ij")
+        base = (I + nn[0] * J).ravel()
+        cells = np.stack([base + a + nn[0] * b for (a, b) in QUAD_CORNERS], axis=1)
     else:
         Z, Y, X = np.meshgrid(axes[2], axes[1], axes[0], indexing="ij")
         coords = np.stack([X.ravel(), Y.ravel(), Z.ravel()], axis=1)
-        nid = lambda i, j, k: i + nn[0] * (j + nn[1] * k)
-        cells = []
-        for k in range(nels[2]):
-            for j in range(nels[1]):
-                for i in range(nels[0]):
-                    cells.append([nid(i + a, j + b, k + c) for (a, b, c) in HEX_CORNERS])
-    return Grid(dim, tuple(nels), tuple(float(s) for s in sizes), coords,
-                np.asarray(cells, dtype=np.int64))
+        K, J, I = np.meshgrid(np.arange(nels[2]), np.arange(nels[1]), np.arange(nels[0]), indexing="ij")
+        base = (I + nn[0] * (J + nn[1] * K)).ravel()
+        cells = np.stack([base + a + nn[0] * (b + nn[1] * c) for (a, b, c) in HEX_CORNERS], axis=1)
+    return Grid(dim, tuple(nels), tuple(float(s) for s in sizes), coords, cells.astype(np.int64))
 
 
 # --------------------------------------------------------------------------
@@ -108,13 +101,12 @@ def dof_numbering(grid: Grid):
     consecutive dofs (metadata.jl:40-50, 116-145; pinned by metadata.jl:79-95).
     Returns node_dofs (dim, nnodes) and cell_dofs (dim*nv, ncells), 0-based."""
     dim = grid.dim
-    node_dofs = -np.ones((dim, grid.nnodes), dtype=np.int64)
-    nxt = 0
-    for c in range(grid.ncells):
-        for n in grid.cells[c]:
-            if node_dofs[0, n] < 0:
-                node_dofs[:, n] = np.arange(nxt, nxt + dim)
-                nxt += dim
+    flat = grid.cells.ravel()                      # visiting order: cell-major, local order
+    _, first = np.unique(flat, return_index=True)  # first visit of every node
+    order = np.argsort(first, kind="stable")       # nodes sorted by first visit
+    rank = np.empty(grid.nnodes, dtype=np.int64)
+    rank[order] = np.arange(grid.nnodes)
+    node_dofs = dim * rank[None, :] + np.arange(dim)[:, None]
     nv = grid.cells.shape[1]
     cell_dofs = np.empty((dim * nv, grid.ncells), dtype=np.int64)
     for a in range(nv):
@@ -169,6 +161,10 @@ def _approx(a, b):
     return abs(a - b) <= math.sqrt(np.finfo(np.float64).eps) * max(abs(a), abs(b))
 
 
+def _approx_v(a, b):
+    return np.abs(a - b) <= math.sqrt(np.finfo(np.float64).eps) * np.maximum(np.abs(a), abs(b))
+
+
 def point_load_cantilever(nels, sizes, E=1.0, nu=0.3, force=1.0,
                           load="reference_first_node", plane_stress=False) -> Problem:
     """problem_types.jl:162-231.  Left face clamped (all components); load
@@ -181,15 +177,14 @@ def point_load_cantilever(nels, sizes, E=1.0, nu=0.3, force=1.0,
     g = rectilinear_grid(nels, sizes)
     node_dofs, cell_dofs = dof_numbering(g)
     lo, hi = np.zeros(dim), np.array(nels) * np.array(sizes, dtype=float)
-    left = [n for n in range(g.nnodes) if _approx(g.coords[n, 0], lo[0]) or g.coords[n, 0] == lo[0]]
-    fixed = sorted(int(node_dofs[d, n]) for n in left for d in range(dim))
+    x = g.coords
+    left = np.nonzero(_approx_v(x[:, 0], lo[0]))[0]
+    fixed = np.sort(node_dofs[:, left].ravel())
     midy = (lo[1] + hi[1]) / 2
-    cand = [n for n in range(g.nnodes)
-            if _approx(g.coords[n, 0], hi[0]) and _approx(g.coords[n, 1], midy)]
+    sel = _approx_v(x[:, 0], hi[0]) & _approx_v(x[:, 1], midy)
     if load == "face_centre" and dim == 3:
-        midz = (lo[2] + hi[2]) / 2
-        cand = [n for n in cand if _approx(g.coords[n, 2], midz)]
-    fnode = cand[0]
+        sel &= _approx_v(x[:, 2], (lo[2] + hi[2]) / 2)
+    fnode = int(np.nonzero(sel)[0][0])          # first node of the ordered node set
     f = np.zeros(node_dofs.size)
     fdof = int(node_dofs[1, fnode])
     f[fdof] = -force
@@ -206,19 +201,14 @@ def half_mbb(nels, sizes, E=1.0, nu=0.3, force=1.0, plane_stress=False) -> Probl
     node_dofs, cell_dofs = dof_numbering(g)
     lo, hi = np.zeros(dim), np.array(nels) * np.array(sizes, dtype=float)
     x = g.coords
-    fixed = set()
-    for n in range(g.nnodes):
-        if x[n, 0] == lo[0] or _approx(x[n, 0], lo[0]):
-            fixed.add(int(node_dofs[0, n]))
-        if (x[n, 1] == lo[1] or _approx(x[n, 1], lo[1])) and _approx(x[n, 0], hi[0]):
-            fixed.add(int(node_dofs[1, n]))
-    cand = [n for n in range(g.nnodes)
-            if _approx(x[n, 1], hi[1]) and (x[n, 0] == lo[0] or _approx(x[n, 0], lo[0]))]
-    fnode = cand[0]
+    f1 = node_dofs[0, np.nonzero(_approx_v(x[:, 0], lo[0]))[0]]
+    f2 = node_dofs[1, np.nonzero(_approx_v(x[:, 1], lo[1]) & _approx_v(x[:, 0], hi[0]))[0]]
+    fixed = np.unique(np.concatenate([f1, f2]))
+    fnode = int(np.nonzero(_approx_v(x[:, 1], hi[1]) & _approx_v(x[:, 0], lo[0]))[0][0])
     f = np.zeros(node_dofs.size)
     fdof = int(node_dofs[1, fnode])
     f[fdof] = -force
-    return Problem(g, E, nu, force, node_dofs, cell_dofs, np.asarray(sorted(fixed), dtype=np.int64),
+    return Problem(g, E, nu, force, node_dofs, cell_dofs, np.asarray(fixed, dtype=np.int64),
                    f, fdof, fnode, plane_stress)
 
 

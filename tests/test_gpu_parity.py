@@ -46,8 +46,12 @@ def test_matvec_matches_oracle(tg, O, nels, kind):
                                        ((7, 4, 6), "cant")])
 @pytest.mark.parametrize("precision", ["fp64", "fp32_ir"])
 def test_solve_matches_direct(tg, O, nels, kind, precision):
+    """FP64 PCG stops on its recurrence residual (as IterativeSolvers' cg!), FP32-IR
+    on the FP64 true residual, whose rounding floor is near 1e-13 here: the IR case
+    is asked for 1e-11."""
     p, op = make(tg, O, nels, kind)
-    s = tg.FEASolver(tg.GB300Solver, p, xmin=1e-3, penalty=tg.PowerPenaltyFun(3.0), rtol=1e-12, abstol=0.0,
+    rtol = 1e-12 if precision == "fp64" else 1e-11
+    s = tg.FEASolver(tg.GB300Solver, p, xmin=1e-3, penalty=tg.PowerPenaltyFun(3.0), rtol=rtol, abstol=0.0,
                      cg_max_iter=20000, precision=precision)
     rng = np.random.default_rng(2)
     s.vars = rng.uniform(0.2, 1.0, p.ncells)
@@ -57,7 +61,7 @@ def test_solve_matches_direct(tg, O, nels, kind, precision):
     ud = O.direct_solve(st)
     u = s.u
     assert np.linalg.norm(u - ud) / np.linalg.norm(ud) < 1e-8
-    assert s.last_stats.rel_residual <= 1e-12 * 1.0001
+    assert s.last_stats.rel_residual <= rtol * 1.0001
     s.close()
 
 

@@ -378,6 +378,7 @@ int solve_fp32_ir(tog_handle* h, double rtol, double abstol, int maxit, int warm
     int inner_total = 0, outer = 0, status = TOG_OK;
     double res = 0.0;
     const int max_outer = 60;
+    double hist[3] = {INFINITY, INFINITY, INFINITY};   // true residuals of the last outer steps
     for (;;) {
         // FP64 true residual r = f - K u
         launch_matvec<double, MV_RESID>(h, h->stream, h->d_u, h->d_r64, h->d_f);
@@ -389,7 +390,12 @@ int solve_fp32_ir(tog_handle* h, double rtol, double abstol, int maxit, int warm
             break;
         }
         if (res <= tol) break;
-        if (outer >= max_outer || inner_total >= maxit) {
+        // stop when the FP64 residual has stalled (rounding floor above tol)
+        const bool stalled = outer >= 3 && res > 0.5 * hist[2];
+        hist[2] = hist[1];
+        hist[1] = hist[0];
+        hist[0] = res;
+        if (outer >= max_outer || inner_total >= maxit || stalled) {
             status = TOG_NOT_CONVERGED;
             break;
         }
