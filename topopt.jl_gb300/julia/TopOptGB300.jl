@@ -1,0 +1,264 @@
+"""
+    TopOptGB300
+
+Julia binding of libtopopt_gb300.so: a GB300 drop-in for TopOpt.jl's SIMP
+compliance loop.  `FEASolver(GB300Solver, problem; xmin, penalty, ...)` returns
+a solver whose `solver()` call, `ComplianceFun`, `VolumeFun`,
+`DensityFilterFun` and `SensFilterFun` run on the GPU through `ccall`; the
+design vector stays a plain `Vector{Float64}` on the host side of every call,
+as in the reference.  Plug-in points used (TopOpt.jl paths):
+
+  * `AbstractLinearSolver` (src/FEA/solvers_api.jl:44) -> `GB300Solver`
+  * `FEASolver(::Type{S}, problem; kw...)` (solvers_api.jl:599-603) -> a
+    `GB300FEASolver <: AbstractFEASolver` that never builds the E copies of Ke
+    nor the sparse K (solvers_api.jl:492-494)
+  * `ComplianceFun` call (src/Functions/compliance.jl:58-70); the generic rrule
+    (compliance.jl:72-76) then returns `comp.grad`
+  * `AbstractDensityFilter` / `AbstractSensFilter` subtypes with call + rrule
+    (src/CheqFilters/CheqFilters.jl:34-41)
+
+Indices cross the boundary 0-based (Julia dof d is d-1 in C).
+"""
+module TopOptGB300
+
+using TopOpt
+using TopOpt: PseudoDensities
+using TopOpt.FEA: AbstractLinearSolver, AbstractFEASolver
+using TopOpt.TopOptProblems: StiffnessTopOptProblem, getdh, getncells
+using TopOpt.CheqFilters: AbstractDensityFilter, AbstractSensFilter
+using TopOpt.Functions: ComplianceFun, VolumeFun
+using TopOpt.Utilities: PowerPenaltyFun, getpenalty
+using ChainRulesCore
+using Ferrite
+
+export GB300Solver, GB300FEASolver, GB300DensityFilter, GB300SensFilter, oc_update!, simp_step!
+
+const libtog = joinpath(@__DIR__, "..", "libtopopt_gb300.so")
+
+const TOG_OK = Cint(0)
+const TOG_NOT_CONVERGED = Cint(3)
+const TOG_FP64 = Cint(0)
+const TOG_FP32_IR = Cint(1)
+
+struct GB300Solver <: AbstractLinearSolver end
+
+struct ProblemDesc
+    dim::Int32
+    nel::NTuple{3,Int32}
+    size::NTuple{3,Float64}
+    E::Float64
+    nu::Float64
+    plane_stress::Int32
+    xmin::Float64
+    penalty::Float64
+end
+
+mutable struct SolveStats
+    status::Int32
+    iterations::Int32
+    outer_iterations::Int32
+    reserved::Int32
+    rel_residual::Float64
+    abs_residual::Float64
+end
+SolveStats() = SolveStats(0, 0, 0, 0, 0.0, 0.0)
+
+last_error() = unsafe_string(ccall((:tog_last_error, libtog), Cstring, ()))
+
+function check(code::Cint)
+    code == TOG_OK && return nothing
+    msg = last_error()
+    code == Cint(1) && throw(ArgumentError(msg))
+    code == TOG_NOT_CONVERGED && (@warn "GB300 PCG: $msg"; return nothing)  # cg! is silent at maxiter
+    return error("libtopopt_gb300: $msg (status $code)")
+end
+
+mutable struct GB300FEASolver{T,TP<:StiffnessTopOptProblem} <: AbstractFEASolver
+    problem::TP
+    handle::Ptr{Cvoid}
+    vars::Vector{T}
+    u::Vector{T}
+    penalty::PowerPenaltyFun{T}
+    xmin::T
+    cg_max_iter::Int
+    abstol::T
+    rtol::T
+    precision::Cint
+    warm_start::Bool
+    stats::SolveStats
+end
+
+"""
+    FEASolver(GB300Solver, problem; xmin=1e-3, penalty=PowerPenaltyFun(1.0),
+              cg_max_iter=700, abstol=1e-7, rtol=sqrt(eps()), precision=:fp64,
+              warm_start=false)
+
+Same keywords and defaults as the reference's `FEASolver` (solvers_api.jl:468-489),
+plus `rtol` (IterativeSolvers' reltol, exposed) and `precision` (`:fp64` or
+`:fp32_ir`).  Inhomogeneous Dirichlet BCs are rejected as by CGMatrixFreeSolver.
+"""
+function TopOpt.FEA.FEASolver(::Type{GB300Solver}, problem::StiffnessTopOptProblem{dim,T};
+                              xmin=T(1) / 1000, penalty=PowerPenaltyFun{T}(1), cg_max_iter=700,
+                              abstol=T(1e-7), rtol=sqrt(eps(T)), precision=:fp64, warm_start=false,
+                              kwargs...) where {dim,T}
+    ch = problem.ch
+    any(!=(0), ch.inhomogeneities) && throw(ArgumentError(
+        "GB300Solver supports homogeneous Dirichlet BCs only (as CGMatrixFreeSolver)"))
+    rg = problem.rect_grid
+    nel = ntuple(i -> i <= dim ? Int32(rg.nels[i]) : Int32(1), 3)
+    sz = ntuple(i -> i <= dim ? Float64(rg.sizes[i]) : 1.0, 3)
+    desc = Ref(ProblemDesc(Int32(dim), nel, sz, Float64(problem.E), Float64(problem.ν), Int32(0),
+                           Float64(xmin), Float64(penalty.p)))
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:tog_create, libtog), Cint, (Ref{ProblemDesc}, Ref{Ptr{Cvoid}}), desc, h))
+    fixed = Int32.(ch.prescribed_dofs .- 1)
+    check(ccall((:tog_set_fixed_dofs, libtog), Cint, (Ptr{Cvoid}, Int64, Ptr{Int32}), h[], length(fixed), fixed))
+    f = Vector{Float64}(TopOpt.TopOptProblems.make_cload(problem))
+    check(ccall((:tog_set_rhs, libtog), Cint, (Ptr{Cvoid}, Ptr{Float64}), h[], f))
+    nc = getncells(problem)
+    prec = precision === :fp32_ir ? TOG_FP32_IR : TOG_FP64
+    s = GB300FEASolver{T,typeof(problem)}(problem, h[], ones(T, nc), zeros(T, length(f)), penalty, T(xmin),
+                                          cg_max_iter, T(abstol), T(rtol), prec, warm_start, SolveStats())
+    finalizer(s) do x
+        x.handle == C_NULL || ccall((:tog_destroy, libtog), Cint, (Ptr{Cvoid},), x.handle)
+        x.handle = C_NULL
+    end
+    return s
+end
+
+TopOpt.Utilities.getpenalty(s::GB300FEASolver) = s.penalty
+function TopOpt.Utilities.setpenalty!(s::GB300FEASolver, p)
+    s.penalty = p isa PowerPenaltyFun ? p : PowerPenaltyFun(oftype(s.xmin, p))
+    check(ccall((:tog_set_penalty, libtog), Cint, (Ptr{Cvoid}, Float64), s.handle, s.penalty.p))
+    return s
+end
+
+"""`solver()`: solve K(vars) u = f on the GPU (replaces solvers_api.jl:285-374)."""
+function (s::GB300FEASolver)(args...; kwargs...)
+    length(s.vars) == getncells(s.problem) || throw(DimensionMismatch("vars"))
+    check(ccall((:tog_set_vars, libtog), Cint, (Ptr{Cvoid}, Ptr{Float64}), s.handle, s.vars))
+    check(ccall((:tog_solve, libtog), Cint,
+                (Ptr{Cvoid}, Cint, Float64, Float64, Int32, Int32, Ref{SolveStats}),
+                s.handle, s.precision, s.rtol, s.abstol, s.cg_max_iter, Int32(s.warm_start), s.stats))
+    check(ccall((:tog_get_u, libtog), Cint, (Ptr{Cvoid}, Ptr{Float64}), s.handle, s.u))
+    return nothing
+end
+
+# ComplianceFun(solver) builds cell_comp / grad from the grid only; its call is specialised here.
+function (o::ComplianceFun{T,<:GB300FEASolver})(x::PseudoDensities) where {T}
+    s = o.solver
+    s.vars .= x.x
+    s()
+    c = Ref{Float64}(0.0)
+    check(ccall((:tog_compliance, libtog), Cint, (Ptr{Cvoid}, Ref{Float64}, Ptr{Float64}), s.handle, c, o.grad))
+    return c[]
+end
+
+function TopOpt.Functions.VolumeFun(s::GB300FEASolver{T}; fraction=true) where {T}
+    rg = s.problem.rect_grid
+    cellvolumes = fill(T(prod(rg.sizes)), getncells(s.problem))
+    total = sum(cellvolumes)
+    grad = fraction ? cellvolumes ./ total : copy(cellvolumes)
+    return VolumeFun(s, cellvolumes, grad, total, fraction)
+end
+
+struct GB300DensityFilter{TS<:GB300FEASolver} <: AbstractDensityFilter
+    solver::TS
+    rmin::Float64
+end
+struct GB300SensFilter{TS<:GB300FEASolver} <: AbstractSensFilter
+    solver::TS
+    rmin::Float64
+end
+
+function _filter_setup(s::GB300FEASolver, rmin)
+    check(ccall((:tog_filter_setup, libtog), Cint, (Ptr{Cvoid}, Float64), s.handle, Float64(rmin)))
+end
+function _filter_apply(s::GB300FEASolver, op::Integer, v::AbstractVector)
+    out = similar(v, Float64)
+    check(ccall((:tog_filter_apply, libtog), Cint, (Ptr{Cvoid}, Int32, Ptr{Float64}, Ptr{Float64}),
+                s.handle, Int32(op), Vector{Float64}(v), out))
+    return out
+end
+
+"""`DensityFilterFun(solver::GB300FEASolver; rmin)` (density_filter.jl:25-33)."""
+function TopOpt.CheqFilters.DensityFilterFun(s::GB300FEASolver, rmin::Real, args...)
+    _filter_setup(s, rmin)
+    return GB300DensityFilter(s, Float64(rmin))
+end
+TopOpt.CheqFilters.DensityFilterFun(s::GB300FEASolver; rmin) = TopOpt.CheqFilters.DensityFilterFun(s, rmin)
+function TopOpt.CheqFilters.SensFilterFun(s::GB300FEASolver, rmin::Real, args...)
+    _filter_setup(s, rmin)
+    return GB300SensFilter(s, Float64(rmin))
+end
+TopOpt.CheqFilters.SensFilterFun(s::GB300FEASolver; rmin) = TopOpt.CheqFilters.SensFilterFun(s, rmin)
+
+(f::GB300DensityFilter)(x::PseudoDensities{I,P}) where {I,P} = PseudoDensities{I,P,true}(_filter_apply(f.solver, 0, x.x))
+function ChainRulesCore.rrule(f::GB300DensityFilter, x::PseudoDensities)
+    return f(x), Δ -> begin
+        _Δ = ChainRulesCore.unthunk(Δ)
+        _Δ = hasproperty(_Δ, :x) ? _Δ.x : _Δ
+        (NoTangent(), Tangent{typeof(x)}(; x=_filter_apply(f.solver, 1, _Δ)))
+    end
+end
+(f::GB300SensFilter)(x::PseudoDensities{I,P}) where {I,P} = PseudoDensities{I,P,true}(x.x)
+function ChainRulesCore.rrule(f::GB300SensFilter, x::PseudoDensities)
+    return x, Δ -> begin
+        _Δ = ChainRulesCore.unthunk(Δ)
+        _Δ = hasproperty(_Δ, :x) ? _Δ.x : _Δ
+        (NoTangent(), Tangent{typeof(x)}(; x=_filter_apply(f.solver, 0, _Δ)))
+    end
+end
+
+"""
+    oc_update!(xnew, solver, x, dc, dv, w; volfrac, move=0.2) -> (change, λ)
+
+Optimality-criteria update on the GPU (published OC method; TopOpt.jl has none).
+"""
+function oc_update!(xnew::Vector{Float64}, s::GB300FEASolver, x, dc, dv, w; volfrac, move=0.2)
+    ch, lam = Ref(0.0), Ref(0.0)
+    check(ccall((:tog_oc_update, libtog), Cint,
+                (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Float64, Float64,
+                 Ptr{Float64}, Ref{Float64}, Ref{Float64}),
+                s.handle, Vector{Float64}(x), Vector{Float64}(dc), Vector{Float64}(dv), Vector{Float64}(w),
+                Float64(volfrac), Float64(move), xnew, ch, lam))
+    return ch[], lam[]
+end
+
+mutable struct IterStats
+    compliance::Float64
+    volume::Float64
+    change::Float64
+    lambda::Float64
+    cg_iterations::Int32
+    outer_iterations::Int32
+    oc_steps::Int32
+    status::Int32
+    rel_residual::Float64
+end
+IterStats() = IterStats(0, 0, 0, 0, 0, 0, 0, 0, 0)
+
+"""
+    simp_init!(solver, x0; volfrac, rmin, filter=:density, move=0.2)
+    simp_step!(solver) -> IterStats
+
+Device-resident SIMP loop: one call per design iteration, the design stays in HBM.
+"""
+function simp_init!(s::GB300FEASolver, x0::AbstractVector; volfrac, rmin=0.0, filter=:density, move=0.2)
+    kind = filter === :density ? Int32(1) : filter === :sens ? Int32(2) : Int32(0)
+    check(ccall((:tog_simp_init, libtog), Cint, (Ptr{Cvoid}, Int32, Float64, Float64, Float64, Ptr{Float64}),
+                s.handle, kind, Float64(rmin), Float64(volfrac), Float64(move), Vector{Float64}(x0)))
+end
+function simp_step!(s::GB300FEASolver)
+    st = Ref(IterStats())
+    check(ccall((:tog_simp_step, libtog), Cint, (Ptr{Cvoid}, Cint, Float64, Int32, Int32, Ref{IterStats}),
+                s.handle, s.precision, s.rtol, Int32(s.cg_max_iter), Int32(s.warm_start), st))
+    return st[]
+end
+function design(s::GB300FEASolver)
+    x = zeros(getncells(s.problem))
+    check(ccall((:tog_get_design, libtog), Cint, (Ptr{Cvoid}, Ptr{Float64}), s.handle, x))
+    return x
+end
+
+end # module
