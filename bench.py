@@ -46,13 +46,14 @@ def read_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
-def read_traffic():
-    """dram bytes per launch of the PCG operator kernel from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "k_matvec3_fp32_pcg_160x80x80.md")
+def read_traffic(ncells):
+    """DRAM bytes per launch of the PCG operator kernel: the committed ncu summary's
+    bytes per cell (captured on a case larger than L2) scaled by the cell count."""
+    p = os.path.join(ROOT, "profiles", "k_matvec3_fp32_pcg_256x128x128.md")
     try:
         for line in open(p):
-            if line.startswith("traffic_bytes_per_launch:"):
-                return float(line.split(":")[1])
+            if line.startswith("traffic_bytes_per_element:"):
+                return float(line.split(":")[1]) * ncells
     except Exception:
         pass
     return None
@@ -228,6 +229,13 @@ def run_ours(args):
     value = ws * args.steps / t_dev
     clocks = clk.summary()
 
+    if args.no_extra:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": "design_iters/s", "steps": args.steps,
+                              "warmup": args.warmup, "partial": "e2e/fp64/roofline legs skipped (--no-extra)",
+                              "inner_cg_iters_per_step": [int(s.cg_iterations) for s in stats]}), flush=True)
+        return 0
+
     # ---- e2e: same loop through the C ABI with the design in pinned host memory
     xh = torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
     xh[:] = loop.x
@@ -298,7 +306,7 @@ def run_ours(args):
     peaks, src = read_peaks()
     achieved = nbytes.value / t_k / 1e9
     roof = {"bound": "hbm", "kernel": "k_matvec3<float, PCG>", "achieved": achieved, "peak": peaks["hbm_gbs"],
-            "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": read_traffic(),
+            "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": read_traffic(n),
             "algorithmic_bytes_per_launch": nbytes.value, "us_per_launch": t_k * 1e6,
             "peak_source": src + " (MEASURED_PEAKS.json hbm_gbs, burst copy)" if src == "measured" else src}
     solver.close()
@@ -334,6 +342,26 @@ def run_ours(args):
     return 0
 
 
+def run_profile(args):
+    """Small profiling driver: three launches of the FP32 PCG operator kernel on a
+    uniform design (no timing; used under ncu)."""
+    import __graft_entry__ as ge
+    tg = ge.load()
+    L = tg._lib
+    nels = tuple(int(v) for v in args.nels.split(","))
+    prob = tg.PointLoadCantilever(nels, (1.0,) * len(nels), load="face_centre")
+    s = tg.FEASolver(tg.GB300Solver, prob, xmin=XMIN, penalty=tg.PowerPenaltyFun(PEN))
+    s.vars = np.full(prob.ncells, VOLFRAC)
+    s._push_vars()
+    L.check(L.lib().tog_bench_pcg_matvec(s.handle, L.TOG_FP32_IR, 3))
+    L.check(L.lib().tog_bench_pcg_matvec(s.handle, L.TOG_FP64, 1))
+    v = np.empty(prob.ndofs)
+    L.check(L.lib().tog_get_u(s.handle, L.dptr(v)))   # synchronises
+    s.close()
+    print("profile driver ok", nels)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -341,7 +369,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extra", action="store_true", help="skip the e2e, accuracy, FP64 and roofline legs")
+    ap.add_argument("--profile", action="store_true", help="run the small ncu driver instead of the benchmark")
+    ap.add_argument("--nels", default="256,128,128", help="grid of --profile")
     args = ap.parse_args()
+    if args.profile:
+        return run_profile(args)
     if args.warmup < 3:
         log("warmup raised to 3 (timing rule)")
         args.warmup = 3
