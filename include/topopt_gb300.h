@@ -163,6 +163,20 @@ int tog_bench_pcg_matvec(tog_handle* h, int32_t precision, int32_t nlaunch);
 /* Algorithmic bytes moved by one launch of that kernel. */
 int tog_pcg_matvec_bytes(tog_handle* h, int32_t precision, double* bytes);
 
+/* ---- allocation-free OC update: no counterpart in TopOpt.jl ----------------------------
+ * For callers that cannot call cudaMalloc (a framework that owns and pre-partitions all
+ * device memory, a memory-capped service, a loop that must not allocate between
+ * iterations).  Same update as tog_oc_update, on the caller's DEVICE arrays of n cells,
+ * launched on `stream` (cudaStream_t as void*, may be NULL) without a host sync;
+ * result_dev[0..2] = change, lambda, volume.  Allocates nothing: its scratch is a static
+ * device array of the library (about 8.1 MiB on every GPU that loads it, held until exit),
+ * so n must be <= 1,048,576 (TOG_ERR_ARG otherwise).  The first call on a device looks up
+ * the array's address (make it before any stream capture).  Calls share the array; calls
+ * that overlap on the GPU race. */
+int tog_oc_update_noalloc(int64_t n, const double* x_dev, const double* dc_dev, const double* dv_dev,
+                          const double* w_dev, double volfrac, double move, double* xnew_dev, double* result_dev,
+                          void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -2,7 +2,7 @@
 
     python topopt.jl_gb300/build.py
 
-The two translation units are compiled in parallel and linked with the static
+The translation units are compiled in parallel and linked with the static
 CUDA runtime, so the library needs only the NVIDIA driver at run time.
 """
 import os
@@ -31,6 +31,8 @@ def build(verbose=False):
     jobs = [
         [NVCC] + COMMON + ARCH + ["-lineinfo", "-c", os.path.join(CSRC, "tog_api.cu"),
                                   "-o", os.path.join(BUILD, "tog_api.o")] + (["-Xptxas", "-v"] if verbose else []),
+        [NVCC] + COMMON + ARCH + ["-lineinfo", "-c", os.path.join(CSRC, "tog_noalloc.cu"),
+                                  "-o", os.path.join(BUILD, "tog_noalloc.o")],
         [NVCC] + COMMON + ["-x", "c++", "-c", os.path.join(CSRC, "tog_host.cpp"),
                            "-o", os.path.join(BUILD, "tog_host.o")],
     ]
@@ -38,7 +40,7 @@ def build(verbose=False):
         logs = list(ex.map(_run, jobs))
     tmp = LIB + ".tmp"
     _run([NVCC] + ARCH + ["-shared", "-o", tmp, os.path.join(BUILD, "tog_api.o"),
-                          os.path.join(BUILD, "tog_host.o")])
+                          os.path.join(BUILD, "tog_noalloc.o"), os.path.join(BUILD, "tog_host.o")])
     os.replace(tmp, LIB)
     if verbose:
         print("".join(logs))

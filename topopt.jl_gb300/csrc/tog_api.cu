@@ -47,6 +47,8 @@ constexpr int kOcMaxSteps = 100;
 
 }  // namespace
 
+int tog::set_error(int code, const char* msg) { return fail(code, msg); }
+
 struct tog_handle {
     // problem
     int dim = 3;

@@ -65,4 +65,7 @@ struct Dims {
     long long nnodes, ncells;
 };
 
+// Records the message returned by tog_last_error() and returns code.
+int set_error(int code, const char* msg);
+
 }  // namespace tog
