@@ -290,25 +290,33 @@ def run_ours(args):
             "cg_iters_per_step": [int(s.cg_iterations) for s in st64]}
     s64.close()
 
-    # ---- roofline of the dominant kernel: FP32 PCG operator (k_matvec3<float, PCG>)
-    nl = 200
-    L.check(L.lib().tog_bench_pcg_matvec(solver.handle, L.TOG_FP32_IR, 10))
-    torch.cuda.synchronize()
-    h0, h1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with torch.cuda.stream(stream):
-        h0.record(stream)
-        L.check(L.lib().tog_bench_pcg_matvec(solver.handle, L.TOG_FP32_IR, nl))
-        h1.record(stream)
-    torch.cuda.synchronize()
-    t_k = h0.elapsed_time(h1) / 1e3 / nl
-    nbytes = L.C.c_double()
-    L.check(L.lib().tog_pcg_matvec_bytes(solver.handle, L.TOG_FP32_IR, L.C.byref(nbytes)))
+    # ---- roofline of the dominant kernel (FP32 PCG operator, k_mv3<float, PCG>) and of the
+    #      PCG update, each timed alone with CUDA events on the launching stream
     peaks, src = read_peaks()
-    achieved = nbytes.value / t_k / 1e9
-    roof = {"bound": "hbm", "kernel": "k_matvec3<float, PCG>", "achieved": achieved, "peak": peaks["hbm_gbs"],
+
+    def time_kernel(kernel, nl):
+        L.check(L.lib().tog_bench_kernel(solver.handle, kernel, L.TOG_FP32_IR, 10))
+        torch.cuda.synchronize()
+        h0, h1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            h0.record(stream)
+            L.check(L.lib().tog_bench_kernel(solver.handle, kernel, L.TOG_FP32_IR, nl))
+            h1.record(stream)
+        torch.cuda.synchronize()
+        t = h0.elapsed_time(h1) / 1e3 / nl
+        nb = L.C.c_double()
+        L.check(L.lib().tog_kernel_bytes(solver.handle, kernel, L.TOG_FP32_IR, L.C.byref(nb)))
+        return t, nb.value
+
+    t_k, nbytes = time_kernel(0, 200)
+    t_u, ubytes = time_kernel(1, 200)
+    achieved = nbytes / t_k / 1e9
+    roof = {"bound": "hbm", "kernel": "k_mv3<float, PCG>", "achieved": achieved, "peak": peaks["hbm_gbs"],
             "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": read_traffic(n),
-            "algorithmic_bytes_per_launch": nbytes.value, "us_per_launch": t_k * 1e6,
-            "peak_source": src + " (MEASURED_PEAKS.json hbm_gbs, burst copy)" if src == "measured" else src}
+            "algorithmic_bytes_per_launch": nbytes, "us_per_launch": t_k * 1e6,
+            "peak_source": src + " (MEASURED_PEAKS.json hbm_gbs, burst copy)" if src == "measured" else src,
+            "pcg_update": {"kernel": "k_pcg_update3<float>", "us_per_launch": t_u * 1e6,
+                           "achieved_gbs": ubytes / t_u / 1e9, "frac": ubytes / t_u / 1e9 / peaks["hbm_gbs"]}}
     solver.close()
 
     cg = [int(s.cg_iterations) for s in stats]
@@ -343,8 +351,9 @@ def run_ours(args):
 
 
 def run_profile(args):
-    """Small profiling driver: three launches of the FP32 PCG operator kernel on a
-    uniform design (no timing; used under ncu)."""
+    """Small profiling driver: three launches each of the FP32 PCG operator and PCG
+    update kernels, then one FP64 operator launch, on a uniform design (no timing;
+    used under ncu)."""
     import __graft_entry__ as ge
     tg = ge.load()
     L = tg._lib
@@ -353,8 +362,9 @@ def run_profile(args):
     s = tg.FEASolver(tg.GB300Solver, prob, xmin=XMIN, penalty=tg.PowerPenaltyFun(PEN))
     s.vars = np.full(prob.ncells, VOLFRAC)
     s._push_vars()
-    L.check(L.lib().tog_bench_pcg_matvec(s.handle, L.TOG_FP32_IR, 3))
-    L.check(L.lib().tog_bench_pcg_matvec(s.handle, L.TOG_FP64, 1))
+    L.check(L.lib().tog_bench_kernel(s.handle, 0, L.TOG_FP32_IR, 3))
+    L.check(L.lib().tog_bench_kernel(s.handle, 1, L.TOG_FP32_IR, 3))
+    L.check(L.lib().tog_bench_kernel(s.handle, 0, L.TOG_FP64, 1))
     v = np.empty(prob.ndofs)
     L.check(L.lib().tog_get_u(s.handle, L.dptr(v)))   # synchronises
     s.close()

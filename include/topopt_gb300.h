@@ -157,11 +157,13 @@ int tog_set_design(tog_handle* h, const double* x);
 /* Filtered (physical) densities of the last step. */
 int tog_get_physical(tog_handle* h, double* xf);
 
-/* ---- measurement hook: launch the solver's matrix-free PCG kernel n times on the
- *      handle's stream over the handle's own PCG vectors (no host sync). ------------- */
-int tog_bench_pcg_matvec(tog_handle* h, int32_t precision, int32_t nlaunch);
+/* ---- measurement hooks (no reference counterpart) ------------------------------------
+ * Launch one solver kernel nlaunch times on the handle's stream over the handle's own PCG
+ * vectors, starting from a fresh PCG state at r = f, without a host sync:
+ * kernel 0 = the matrix-free PCG operator, 1 = the PCG vector update. */
+int tog_bench_kernel(tog_handle* h, int32_t kernel, int32_t precision, int32_t nlaunch);
 /* Algorithmic bytes moved by one launch of that kernel. */
-int tog_pcg_matvec_bytes(tog_handle* h, int32_t precision, double* bytes);
+int tog_kernel_bytes(tog_handle* h, int32_t kernel, int32_t precision, double* bytes);
 
 /* ---- allocation-free OC update: no counterpart in TopOpt.jl ----------------------------
  * For callers that cannot call cudaMalloc (a framework that owns and pre-partitions all

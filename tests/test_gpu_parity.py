@@ -209,3 +209,38 @@ def test_singular_void_design_reports_failure(tg):
     with pytest.raises(tg.TopOptError):
         s()
     s.close()
+
+
+@pytest.mark.parametrize("lz", ["1", "3", "5", "64"])
+@pytest.mark.parametrize("nels,kind", [((70, 20, 12), "cant"), ((33, 10, 6), "cant"), ((64, 16, 10), "cant"),
+                                       ((33, 9, 7), "mbb")])
+def test_operator_tiling_and_chunking(tg, O, nels, kind, lz, monkeypatch):
+    """The 3D operator splits the grid into 32 x 8 element tiles and z chunks of
+    LZ layers; tile-boundary partial sums travel through side buffers.  Every
+    chunk length must give the oracle's operator and the direct solution."""
+    monkeypatch.setenv("TOG_MV3_LZ", lz)
+    p, op = make(tg, O, nels, kind)
+    s = tg.FEASolver(tg.GB300Solver, p, xmin=1e-3, penalty=tg.PowerPenaltyFun(3.0), rtol=1e-12, abstol=0.0,
+                     cg_max_iter=50000)
+    rng = np.random.default_rng(7)
+    s.vars = rng.uniform(0.05, 1.0, p.ncells)
+    x = rng.standard_normal(p.ndofs)
+    st = O.fea_setup(op, xmin=1e-3, p=3.0)
+    st.vars = s.vars
+    assert rel(s.matvec(x), O.matvec(st, x)) < 1e-12
+    s()
+    ud = O.direct_solve(st)
+    if kind == "mbb":
+        # 3D HalfMBB leaves the z translation free: K is singular and solutions differ by a
+        # rigid shift in z; compare the true residual and the compliance instead
+        u = s.u
+        r = O.matvec(st, u) - np.where(st.free_mask, op.f, 0.0)
+        assert np.linalg.norm(r) <= 1e-10 * np.linalg.norm(op.f)
+        assert abs(op.f @ u - op.f @ ud) <= 1e-8 * abs(op.f @ ud)
+    else:
+        assert np.linalg.norm(s.u - ud) / np.linalg.norm(ud) < 1e-8
+        # the FP32 operator inside refinement on the same tiling (true FP64 residual to 1e-11)
+        s.rtol = 1e-11
+        s(precision="fp32_ir")
+        assert np.linalg.norm(s.u - ud) / np.linalg.norm(ud) < 1e-8
+    s.close()

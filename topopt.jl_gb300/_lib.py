@@ -66,8 +66,8 @@ SIGNATURES = {
     "tog_get_design": (C.c_int, [_H, _D]),
     "tog_set_design": (C.c_int, [_H, _D]),
     "tog_get_physical": (C.c_int, [_H, _D]),
-    "tog_bench_pcg_matvec": (C.c_int, [_H, C.c_int32, C.c_int32]),
-    "tog_pcg_matvec_bytes": (C.c_int, [_H, C.c_int32, _D]),
+    "tog_bench_kernel": (C.c_int, [_H, C.c_int32, C.c_int32, C.c_int32]),
+    "tog_kernel_bytes": (C.c_int, [_H, C.c_int32, C.c_int32, _D]),
     "tog_oc_update_noalloc": (C.c_int, [C.c_int64, _D, _D, _D, _D, C.c_double, C.c_double, _D, _D, C.c_void_p]),
 }
 

@@ -2,7 +2,9 @@
 // One tog_handle = one structured problem resident in HBM: design, densities,
 // element scales, PCG vectors, filter stencil and OC scratch.  The per-iteration
 // host<->device traffic of the device-resident loop is a handful of scalars.
+#include <algorithm>
 #include <atomic>
+#include <cstdlib>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -12,6 +14,8 @@
 #include "../../include/topopt_gb300.h"
 #include "tog_host.h"
 #include "tog_kernels.cuh"
+#include "tog_mv3.cuh"
+#include "tog_mv3x2.cuh"
 
 using namespace tog;
 
@@ -110,6 +114,13 @@ struct tog_handle {
     double *d_x = nullptr, *d_xnew = nullptr, *d_dc = nullptr, *d_dv = nullptr, *d_w = nullptr, *d_grad = nullptr,
            *d_B = nullptr;
     bool simp_ready = false;
+    // 3D operator tiling: tiles of 32 x MV3_BY elements, LZ layers per z chunk
+    int nt[3] = {1, 1, 1};
+    int LZ = 8;
+    bool mv3_scalar = true;    // FP32 operator: k_mv3 (scalar) unless TOG_MV3_KERNEL=pair
+    double ru_delta = 0.1;     // FP32-IR reliable-update trigger: residual reduction factor (TOG_RU_DELTA)
+    float* d_side32[8] = {};
+    double* d_side64[8] = {};
     // graphs
     cudaGraphExec_t g_pcg64 = nullptr, g_pcg32 = nullptr, g_oc = nullptr;
     int graph_nodes_pcg = 0;
@@ -124,6 +135,11 @@ struct tog_handle {
         D.nnodes = nnodes;
         D.ncells = ncells;
         return D;
+    }
+    int upd_blocks() const {   // PCG update grid: a few blocks per SM, grid-stride over node pairs
+        long long b = (nnodes + 2LL * kEwThreads - 1) / (2LL * kEwThreads);
+        const long long cap = (long long)nsm * 4;
+        return (int)std::max(1LL, std::min(b, cap));
     }
     int ew_blocks(long long n) const {
         long long b = (n + kEwThreads - 1) / kEwThreads;
@@ -219,17 +235,65 @@ void fill_common(tog_handle* h, MvArgs<T, DIM>& A) {
     A.partials = h->d_partials;
 }
 
-// Launch one matrix-free operator kernel (mode MV_*) in precision T.
+template <typename T>
+Mv3Args<T> mv3_args(tog_handle* h) {
+    Mv3Args<T> A{};
+    const MvArgs<T, 3> B = mv_args3<T>(h);
+    A.r = B.r;
+    A.P0 = B.P0;
+    A.P1 = B.P1;
+    A.q = B.q;
+    A.escale = B.escale;
+    A.dinv = B.dinv;
+    A.st = B.st;
+    A.M = B.M;
+    A.fixmask = h->d_fixmask;
+    A.partials = h->d_partials;
+    for (int d = 0; d < 3; ++d) {
+        A.nel[d] = h->nel[d];
+        A.nn[d] = h->nn[d];
+        A.nt[d] = h->nt[d];
+    }
+    A.LZ = h->LZ;
+    A.div_nnx = make_fastdiv((unsigned)h->nn[0]);
+    A.div_nny = make_fastdiv((unsigned)h->nn[1]);
+    for (int c = 0; c < 8; ++c)
+        A.side[c] = std::is_same<T, double>::value ? (T*)h->d_side64[c] : (T*)h->d_side32[c];
+    return A;
+}
+
+template <int MODE>
+void launch_mv3x2(tog_handle* h, cudaStream_t s, const Mv3Args<float>& A) {
+    k_mv3x2<MODE><<<dim3(h->nt[0], h->nt[1], h->nt[2]), dim3(32, MX_WARPS), 0, s>>>(A);
+}
+
+template <typename T, int MODE>
+void launch_mv3(tog_handle* h, cudaStream_t s, const Mv3Args<T>& A) {
+    static bool attr_set = false;
+    const int smem = (int)sizeof(Mv3Smem<T>);
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_mv3<T, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        attr_set = true;
+    }
+    k_mv3<T, MODE><<<dim3(h->nt[0], h->nt[1], h->nt[2]), dim3(32, MV3_BY), smem, s>>>(A);
+}
+
+// Launch one matrix-free operator kernel (mode MV_*) in precision T.  3D PLAIN and
+// RESID add the finalize kernel that gathers the tile-boundary partials.
 template <typename T, int MODE>
 void launch_matvec(tog_handle* h, cudaStream_t s, const T* x, T* y, const double* f) {
     if (h->dim == 3) {
-        MvArgs<T, 3> A = mv_args3<T>(h);
-        fill_common<T, 3>(h, A);
+        Mv3Args<T> A = mv3_args<T>(h);
         A.x = x;
-        A.y = y;
-        A.f = f;
         if (MODE == MV_RESID) A.st = h->d_st64;
-        k_matvec3<T, MODE><<<mv3_grid(h), dim3(32, MV_BY), 0, s>>>(A);
+        if (std::is_same<T, float>::value && MODE != MV_RESID && !h->mv3_scalar)
+            launch_mv3x2<MODE == MV_RESID ? MV_PLAIN : MODE>(h, s, *reinterpret_cast<const Mv3Args<float>*>(&A));
+        else
+            launch_mv3<T, MODE>(h, s, A);
+        if (MODE != MV_PCG) {
+            k_mv3_finalize<T, MODE><<<h->ew_blocks(h->nnodes), kEwThreads, 0, s>>>(A, x, y, f, (T)h->meandiag);
+            TOG_LAUNCHED(1);
+        }
     } else {
         MvArgs<T, 2> A = mv_args2<T>(h);
         fill_common<T, 2>(h, A);
@@ -245,21 +309,16 @@ void launch_matvec(tog_handle* h, cudaStream_t s, const T* x, T* y, const double
 template <typename T>
 void launch_pcg_update(tog_handle* h, cudaStream_t s) {
     const int nb = h->ew_blocks(h->nnodes);
-    if (std::is_same<T, double>::value) {
-        if (h->dim == 3)
-            k_pcg_update<double, 3><<<nb, kEwThreads, 0, s>>>(h->d_u, h->d_r64, h->d_p64[0], h->d_p64[1], h->d_q64,
-                                                              h->d_dinv64, h->M3d, h->nnodes, h->d_st64,
-                                                              h->d_partials);
-        else
+    if (h->dim == 3) {
+        Mv3Args<T> A = mv3_args<T>(h);
+        T* x = std::is_same<T, double>::value ? (T*)h->d_u : (T*)h->d_x32;
+        T* r = std::is_same<T, double>::value ? (T*)h->d_r64 : (T*)h->d_r32;
+        k_pcg_update3<T><<<h->upd_blocks(), kEwThreads, 0, s>>>(A, x, r, (T)h->meandiag);
+    } else if (std::is_same<T, double>::value) {
             k_pcg_update<double, 2><<<nb, kEwThreads, 0, s>>>(h->d_u, h->d_r64, h->d_p64[0], h->d_p64[1], h->d_q64,
                                                               h->d_dinv64, h->M2d, h->nnodes, h->d_st64,
                                                               h->d_partials);
     } else {
-        if (h->dim == 3)
-            k_pcg_update<float, 3><<<nb, kEwThreads, 0, s>>>(h->d_x32, h->d_r32, h->d_p32[0], h->d_p32[1], h->d_q32,
-                                                             h->d_dinv32, h->M3f, h->nnodes, h->d_st32,
-                                                             h->d_partials);
-        else
             k_pcg_update<float, 2><<<nb, kEwThreads, 0, s>>>(h->d_x32, h->d_r32, h->d_p32[0], h->d_p32[1], h->d_q32,
                                                              h->d_dinv32, h->M2f, h->nnodes, h->d_st32,
                                                              h->d_partials);
@@ -268,26 +327,27 @@ void launch_pcg_update(tog_handle* h, cudaStream_t s) {
 }
 
 template <typename T>
-void launch_pcg_init(tog_handle* h, cudaStream_t s, int zero_x, double rtol, double abstol, double bnorm2, int maxit) {
+void launch_pcg_init(tog_handle* h, cudaStream_t s, int zero_x, double rtol, double abstol, double bnorm2, int maxit,
+                     double ru_delta2 = 0.0) {
     const int nb = h->ew_blocks(h->nnodes);
     if (std::is_same<T, double>::value) {
         if (h->dim == 3)
             k_pcg_init<double, 3><<<nb, kEwThreads, 0, s>>>(h->d_u, h->d_r64, h->d_p64[0], h->d_p64[1], h->d_dinv64,
                                                             h->M3d, h->nnodes, zero_x, rtol, abstol, bnorm2, maxit,
-                                                            h->d_st64, h->d_partials);
+                                                            h->d_st64, h->d_partials, ru_delta2);
         else
             k_pcg_init<double, 2><<<nb, kEwThreads, 0, s>>>(h->d_u, h->d_r64, h->d_p64[0], h->d_p64[1], h->d_dinv64,
                                                             h->M2d, h->nnodes, zero_x, rtol, abstol, bnorm2, maxit,
-                                                            h->d_st64, h->d_partials);
+                                                            h->d_st64, h->d_partials, ru_delta2);
     } else {
         if (h->dim == 3)
             k_pcg_init<float, 3><<<nb, kEwThreads, 0, s>>>(h->d_x32, h->d_r32, h->d_p32[0], h->d_p32[1],
                                                            h->d_dinv32, h->M3f, h->nnodes, zero_x, rtol, abstol,
-                                                           bnorm2, maxit, h->d_st32, h->d_partials);
+                                                           bnorm2, maxit, h->d_st32, h->d_partials, ru_delta2);
         else
             k_pcg_init<float, 2><<<nb, kEwThreads, 0, s>>>(h->d_x32, h->d_r32, h->d_p32[0], h->d_p32[1],
                                                            h->d_dinv32, h->M2f, h->nnodes, zero_x, rtol, abstol,
-                                                           bnorm2, maxit, h->d_st32, h->d_partials);
+                                                           bnorm2, maxit, h->d_st32, h->d_partials, ru_delta2);
     }
     TOG_LAUNCHED(1);
 }
@@ -373,67 +433,102 @@ int solve_fp64(tog_handle* h, double rtol, double abstol, int maxit, int warm, t
                                                                    : "PCG breakdown (p'Kp <= 0 or NaN)");
 }
 
+// FP32 PCG inside FP64 refinement with reliable updates: the FP32 iteration
+// pauses whenever its residual has dropped by ru_delta since the last update
+// (or looks converged); the host then folds x32 into the FP64 solution,
+// recomputes the FP64 true residual and rescales the FP32 state, keeping the
+// search direction, so the Krylov progress is not thrown away as by a restart.
 int solve_fp32_ir(tog_handle* h, double rtol, double abstol, int maxit, int warm, tog_solve_stats* st) {
     const long long nd = h->ndofs;
     if (!(warm && h->u_valid)) TOG_CUDA(cudaMemsetAsync(h->d_u, 0, nd * sizeof(double), h->stream));
     const double tol = std::fmax(rtol * std::sqrt(h->fnorm2), abstol);
-    int inner_total = 0, outer = 0, status = TOG_OK;
-    double res = 0.0;
-    const int max_outer = 60;
-    double hist[3] = {INFINITY, INFINITY, INFINITY};   // true residuals of the last outer steps
-    for (;;) {
-        // FP64 true residual r = f - K u
+    const int nb = h->ew_blocks(nd);
+    auto resid = [&](double* res) -> int {
         launch_matvec<double, MV_RESID>(h, h->stream, h->d_u, h->d_r64, h->d_f);
         TOG_CUDA(cudaGetLastError());
         TOG_TRY(sync_state(h, h->d_st64));
-        res = std::sqrt(h->h_st->rr);
-        if (!std::isfinite(res)) {
-            status = TOG_BREAKDOWN;
-            break;
-        }
-        if (res <= tol) break;
-        // stop when the FP64 residual has stalled (rounding floor above tol)
-        const bool stalled = outer >= 3 && res > 0.5 * hist[2];
-        hist[2] = hist[1];
-        hist[1] = hist[0];
-        hist[0] = res;
-        if (outer >= max_outer || inner_total >= maxit || stalled) {
-            status = TOG_NOT_CONVERGED;
-            break;
-        }
-        // inner FP32 solve of K d = r / ||r|| to relative tolerance eta
-        const double need = tol / res;
-        const double eta = std::fmin(0.5, std::fmax(1e-4, 0.3 * need));
-        const int nb = h->ew_blocks(nd);
+        *res = std::sqrt(h->h_st->rr);
+        return TOG_OK;
+    };
+    int status = TOG_OK, updates = 0, inner = 0;
+    double res = 0.0;
+    TOG_TRY(resid(&res));
+    if (std::isfinite(res) && res > tol) {
+        double s = res;
         if (h->dim == 3)
             k_ir_scale<3><<<nb, kEwThreads, 0, h->stream>>>(h->d_r64, h->d_r32, nd, h->d_st64);
         else
             k_ir_scale<2><<<nb, kEwThreads, 0, h->stream>>>(h->d_r64, h->d_r32, nd, h->d_st64);
         TOG_LAUNCHED(1);
-        launch_pcg_init<float>(h, h->stream, 1, eta, 0.0, -1.0, maxit - inner_total);
+        launch_pcg_init<float>(h, h->stream, 1, 0.0, tol / s, -1.0, maxit, h->ru_delta * h->ru_delta);
         TOG_CUDA(cudaGetLastError());
-        TOG_TRY(run_pcg<float>(h));
-        const int its = h->h_st->it;
-        const int ist = h->h_st->status;
-        inner_total += its;
-        k_ir_correct<<<nb, kEwThreads, 0, h->stream>>>(h->d_u, h->d_x32, nd, h->d_st64);
-        TOG_LAUNCHED(1);
-        ++outer;
-        if (ist == 4 && its == 0) {
-            status = TOG_BREAKDOWN;
-            break;
+        double best = res;
+        int since_best = 0;
+        for (;;) {
+            TOG_TRY(run_pcg<float>(h));
+            const PcgState s32 = *h->h_st;
+            inner = s32.it;
+            k_ir_correct<<<nb, kEwThreads, 0, h->stream>>>(h->d_u, h->d_x32, nd, s);
+            TOG_LAUNCHED(1);
+            ++updates;
+            TOG_TRY(resid(&res));
+            if (!std::isfinite(res)) {
+                status = TOG_BREAKDOWN;
+                break;
+            }
+            if (res <= tol) break;
+            if (res < 0.5 * best) {
+                best = res;
+                since_best = 0;
+            } else if (++since_best >= 8) {   // FP64 residual stalled above tol
+                status = TOG_NOT_CONVERGED;
+                break;
+            }
+            if (s32.status == 3 || inner >= maxit) {
+                status = TOG_NOT_CONVERGED;
+                break;
+            }
+            if (s32.status == 4) {
+                // breakdown of the FP32 recurrence: restart from the true residual
+                if (h->dim == 3)
+                    k_ir_scale<3><<<nb, kEwThreads, 0, h->stream>>>(h->d_r64, h->d_r32, nd, h->d_st64);
+                else
+                    k_ir_scale<2><<<nb, kEwThreads, 0, h->stream>>>(h->d_r64, h->d_r32, nd, h->d_st64);
+                TOG_LAUNCHED(1);
+                launch_pcg_init<float>(h, h->stream, 1, 0.0, tol / res, -1.0, maxit - inner,
+                                       h->ru_delta * h->ru_delta);
+                s = res;
+                continue;
+            }
+            const double t2 = (tol / res) * (tol / res);
+            if (h->dim == 3)
+                k_ru_rescale<3><<<nb, kEwThreads, 0, h->stream>>>(h->d_r64, h->d_r32, h->d_x32, h->d_p32[0],
+                                                                  h->d_p32[1], h->d_dinv32, h->M3f, h->nnodes, s,
+                                                                  res, t2, h->d_st32, h->d_partials);
+            else
+                k_ru_rescale<2><<<nb, kEwThreads, 0, h->stream>>>(h->d_r64, h->d_r32, h->d_x32, h->d_p32[0],
+                                                                  h->d_p32[1], h->d_dinv32, h->M2f, h->nnodes, s,
+                                                                  res, t2, h->d_st32, h->d_partials);
+            TOG_LAUNCHED(1);
+            TOG_CUDA(cudaGetLastError());
+            s = res;
         }
     }
     h->u_valid = true;
     if (st) {
         st->status = status;
-        st->iterations = inner_total;
-        st->outer_iterations = outer;
+        st->iterations = inner;
+        st->outer_iterations = updates;
         st->abs_residual = res;
         st->rel_residual = h->fnorm2 > 0 ? res / std::sqrt(h->fnorm2) : res;
     }
-    if (status == TOG_NOT_CONVERGED) return fail(status, "FP32-IR did not reach the FP64 tolerance");
-    if (status == TOG_BREAKDOWN) return fail(status, "FP32-IR breakdown");
+    if (status != TOG_OK) {
+        char msg[200];
+        std::snprintf(msg, sizeof msg, "FP32-IR %s: ||f-Ku||/||f|| = %.3e after %d PCG iterations, %d updates",
+                      status == TOG_BREAKDOWN ? "breakdown" : "did not reach the FP64 tolerance",
+                      h->fnorm2 > 0 ? res / std::sqrt(h->fnorm2) : res, inner, updates);
+        return fail(status, msg);
+    }
     return TOG_OK;
 }
 
@@ -661,10 +756,46 @@ int tog_create(const tog_problem_desc* desc, tog_handle** out) {
         return fail(TOG_ERR_CUDA, std::string("CUDA init: ") + cudaGetErrorString(e));
     }
     h->stream = h->own;
+    if (const char* e = std::getenv("TOG_RU_DELTA")) h->ru_delta = std::min(0.9, std::max(1e-6, std::atof(e)));
+    if (dim == 3) {
+        // z-chunk length: minimise (rounds of resident blocks) x (layers + prologue)
+        h->nt[0] = (h->nel[0] + 31) / 32;
+        h->nt[1] = (h->nel[1] + MV3_BY - 1) / MV3_BY;
+        const long long txy = (long long)h->nt[0] * h->nt[1];
+        if (const char* e = std::getenv("TOG_MV3_KERNEL")) h->mv3_scalar = std::string(e) != "pair";
+        int occ = 0;
+        cudaError_t oe;
+        if (h->mv3_scalar) {
+            cudaFuncSetAttribute(k_mv3<float, MV_PCG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)sizeof(Mv3Smem<float>));
+            oe = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_mv3<float, MV_PCG>, 32 * MV3_BY,
+                                                               sizeof(Mv3Smem<float>));
+        } else {
+            oe = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_mv3x2<MV_PCG>, 32 * MX_WARPS, 0);
+        }
+        if (oe != cudaSuccess || occ < 1) occ = 1;
+        const long long slots = (long long)h->nsm * occ;
+        int best = h->nel[2];
+        double best_cost = 1e300;
+        for (int lz = 2; lz <= h->nel[2]; ++lz) {
+            const long long blocks = txy * ((h->nel[2] + lz - 1) / lz);
+            const double cost = (double)((blocks + slots - 1) / slots) * (lz + 2);
+            if (cost < best_cost) {
+                best_cost = cost;
+                best = lz;
+            }
+        }
+        int lz = best;
+        if (const char* e = std::getenv("TOG_MV3_LZ")) lz = std::max(1, std::atoi(e));
+        h->LZ = lz;
+        h->nt[2] = (h->nel[2] + lz - 1) / lz;
+    }
     const long long N = h->ndofs, NN = h->nnodes, NC = h->ncells;
     // partial-sum buffer: enough for the largest grid of any reducing kernel
     const dim3 g3 = mv3_grid(h), g2 = mv2_grid(h);
     size_t maxb = (size_t)g3.x * g3.y * g3.z;
+    maxb = std::max(maxb, (size_t)h->nt[0] * h->nt[1] * h->nt[2]);
+    maxb = std::max(maxb, (size_t)((h->nnodes + kEwThreads - 1) / kEwThreads));
     maxb = std::max(maxb, (size_t)g2.x * g2.y);
     maxb = std::max(maxb, (size_t)h->nsm * 8);
     h->npartials = maxb * 4;
@@ -702,6 +833,12 @@ int tog_create(const tog_problem_desc* desc, tog_handle** out) {
     A(dalloc(&h->d_cnt, 8));
     A(dalloc(&h->d_scalar, 8));
     A(dalloc(&h->d_invW, NC));
+    if (dim == 3)
+        for (int c = 1; c < 8; ++c) {
+            const long long cnt = 3 * std::max(1LL, side_count(c, h->nn, h->nt));
+            A(dalloc(&h->d_side32[c], cnt));
+            A(dalloc(&h->d_side64[c], cnt));
+        }
     if (rc == TOG_OK) {
         h->d_x = h->d_cell[0];
         h->d_xnew = h->d_cell[1];
@@ -759,6 +896,10 @@ int tog_destroy(tog_handle* h) {
         if (p) cudaFree(p);
     for (int i = 0; i < 6; ++i)
         if (h->d_cell[i]) cudaFree(h->d_cell[i]);
+    for (int c = 0; c < 8; ++c) {
+        if (h->d_side32[c]) cudaFree(h->d_side32[c]);
+        if (h->d_side64[c]) cudaFree(h->d_side64[c]);
+    }
     if (h->h_st) cudaFreeHost(h->h_st);
     if (h->h_oc) cudaFreeHost(h->h_oc);
     if (h->h_scalar) cudaFreeHost(h->h_scalar);
@@ -835,9 +976,9 @@ int tog_matvec(tog_handle* h, const double* x, double* y) {
     if (!x || !y) return fail(TOG_ERR_ARG, "null vector");
     TOG_TRY(refresh_scales(h));
     TOG_TRY(upload_dofs(h, x, h->d_p64[0]));
-    launch_matvec<double, MV_PLAIN>(h, h->stream, h->d_p64[0], h->d_q64, nullptr);
+    launch_matvec<double, MV_PLAIN>(h, h->stream, h->d_p64[0], h->d_r64, nullptr);
     TOG_CUDA(cudaGetLastError());
-    return download_dofs(h, h->d_q64, y);
+    return download_dofs(h, h->d_r64, y);
 }
 
 int tog_solve(tog_handle* h, int32_t precision, double rtol, double abstol, int32_t maxiter, int32_t warm_start,
@@ -1028,17 +1169,23 @@ int tog_get_physical(tog_handle* h, double* xf) {
     return TOG_OK;
 }
 
-int tog_bench_pcg_matvec(tog_handle* h, int32_t precision, int32_t nlaunch) {
+int tog_bench_kernel(tog_handle* h, int32_t kernel, int32_t precision, int32_t nlaunch) {
     TOG_TRY(check_handle(h));
-    if (nlaunch < 0) return fail(TOG_ERR_ARG, "nlaunch < 0");
+    if (nlaunch < 0 || kernel < 0 || kernel > 1) return fail(TOG_ERR_ARG, "bad kernel id or nlaunch");
     TOG_TRY(refresh_scales(h));
     if (h->fnorm2 <= 0) return fail(TOG_ERR_STATE, "set a non-zero rhs first");
+    // fresh PCG state from r = f (maxit huge, tolerance 0: every launch does full work)
+    TOG_CUDA(cudaMemcpyAsync(h->d_r64, h->d_f, h->ndofs * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
     if (precision == TOG_FP64) {
-        TOG_CUDA(cudaMemcpyAsync(h->d_r64, h->d_f, h->ndofs * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
-        launch_pcg_init<double>(h, h->stream, 0, 0.0, 0.0, h->fnorm2, 1 << 30);
-        for (int i = 0; i < nlaunch; ++i) launch_matvec<double, MV_PCG>(h, h->stream, nullptr, nullptr, nullptr);
+        launch_pcg_init<double>(h, h->stream, 1, 0.0, 0.0, h->fnorm2, 1 << 30);
+        launch_matvec<double, MV_PCG>(h, h->stream, nullptr, nullptr, nullptr);
+        for (int i = 0; i < nlaunch; ++i) {
+            if (kernel == 0)
+                launch_matvec<double, MV_PCG>(h, h->stream, nullptr, nullptr, nullptr);
+            else
+                launch_pcg_update<double>(h, h->stream);
+        }
     } else {
-        TOG_CUDA(cudaMemcpyAsync(h->d_r64, h->d_f, h->ndofs * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
         TOG_CUDA(cudaMemcpyAsync(&h->d_st64->rr, &h->fnorm2, sizeof(double), cudaMemcpyHostToDevice, h->stream));
         TOG_CUDA(cudaStreamSynchronize(h->stream));
         const int nb = h->ew_blocks(h->ndofs);
@@ -1048,19 +1195,27 @@ int tog_bench_pcg_matvec(tog_handle* h, int32_t precision, int32_t nlaunch) {
             k_ir_scale<2><<<nb, kEwThreads, 0, h->stream>>>(h->d_r64, h->d_r32, h->ndofs, h->d_st64);
         TOG_LAUNCHED(1);
         launch_pcg_init<float>(h, h->stream, 1, 0.0, 0.0, -1.0, 1 << 30);
-        for (int i = 0; i < nlaunch; ++i) launch_matvec<float, MV_PCG>(h, h->stream, nullptr, nullptr, nullptr);
+        launch_matvec<float, MV_PCG>(h, h->stream, nullptr, nullptr, nullptr);
+        for (int i = 0; i < nlaunch; ++i) {
+            if (kernel == 0)
+                launch_matvec<float, MV_PCG>(h, h->stream, nullptr, nullptr, nullptr);
+            else
+                launch_pcg_update<float>(h, h->stream);
+        }
     }
     TOG_CUDA(cudaGetLastError());
     return TOG_OK;
 }
 
-int tog_pcg_matvec_bytes(tog_handle* h, int32_t precision, double* bytes) {
+int tog_kernel_bytes(tog_handle* h, int32_t kernel, int32_t precision, double* bytes) {
     TOG_TRY(check_handle(h));
-    if (!bytes) return fail(TOG_ERR_ARG, "null output");
+    if (!bytes || kernel < 0 || kernel > 1) return fail(TOG_ERR_ARG, "bad kernel id or null output");
     const double s = precision == TOG_FP64 ? 8.0 : 4.0;
-    // reads r, p_old (N each), dinv (per node), E_e (per cell), fixmask (1 B per node);
-    // writes p, q (N each)
-    *bytes = 4.0 * s * (double)h->ndofs + s * (double)h->nnodes + s * (double)h->ncells + (double)h->nnodes;
+    const double N = (double)h->ndofs, Nn = (double)h->nnodes, E = (double)h->ncells;
+    if (kernel == 0)   // reads r, p_old, D^-1, E_e, mask; writes p, q
+        *bytes = 4.0 * s * N + s * Nn + s * E + Nn;
+    else               // reads q, p, x, r, D^-1, mask; writes x, r
+        *bytes = 6.0 * s * N + s * Nn + Nn;
     return TOG_OK;
 }
 

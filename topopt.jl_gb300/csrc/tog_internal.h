@@ -47,8 +47,11 @@ struct PcgState {
     int it;          // completed iterations
     int done;        // 1 = stop (converged, breakdown or maxit)
     int maxit;
-    int status;      // 0 running/converged, 3 = not converged at maxit, 4 = breakdown
+    int status;      // 0 running/converged, 3 = not converged at maxit, 4 = breakdown,
+                     // 6 = paused for a reliable update
     unsigned cnt[4]; // last-block counters
+    double rr_max;   // largest ||r||^2 since the last reliable update
+    double ru_delta2;// pause when ||r||^2 < ru_delta2 * rr_max (0 = never)
 };
 
 struct OcState {

@@ -459,7 +459,11 @@ __global__ void __launch_bounds__(256) k_pcg_update(T* __restrict__ x, T* __rest
             } else if (it + 1 >= st->maxit) {
                 st->status = 3;
                 st->done = 1;
+            } else if (tot[1] < st->ru_delta2 * st->rr_max) {
+                st->status = 6;
+                st->done = 1;
             }
+            st->rr_max = fmax(st->rr_max, tot[1]);
         }
     }
 }
@@ -472,7 +476,7 @@ __global__ void __launch_bounds__(256) k_pcg_init(T* __restrict__ x, const T* __
                                                   T* __restrict__ P1, const T* __restrict__ dinv,
                                                   const Modal<T, DIM> M, long long nnodes, int zero_x, double rtol,
                                                   double abstol, double bnorm2, int maxit, PcgState* st,
-                                                  double* partials) {
+                                                  double* partials, double ru_delta2) {
     T arz = T(0), arr = T(0);
     for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < nnodes;
          n += (long long)gridDim.x * blockDim.x) {
@@ -505,6 +509,8 @@ __global__ void __launch_bounds__(256) k_pcg_init(T* __restrict__ x, const T* __
             st->done = (tot[1] <= st->tol2 || maxit <= 0) ? 1 : 0;
             if (maxit <= 0 && tot[1] > st->tol2) st->status = 3;
             st->pq = 0.0;
+            st->rr_max = tot[1];
+            st->ru_delta2 = ru_delta2;
         }
     }
 }
@@ -518,13 +524,55 @@ __global__ void __launch_bounds__(256) k_ir_scale(const double* __restrict__ r64
          i += (long long)gridDim.x * blockDim.x)
         r32[i] = (float)(r64[i] * s);
 }
-// u64 += ||r64|| * x32
+// u64 += s * x32
 __global__ void __launch_bounds__(256) k_ir_correct(double* __restrict__ u, const float* __restrict__ x32,
-                                                    long long ndofs, const PcgState* st64) {
-    const double s = sqrt(st64->rr);
+                                                    long long ndofs, double s) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ndofs;
          i += (long long)gridDim.x * blockDim.x)
         u[i] = fma(s, (double)x32[i], u[i]);
+}
+
+// Reliable update of the FP32 PCG: r32 = r64 / s_new (the FP64 true residual),
+// x32 = 0, the last direction rescaled by s_old / s_new, and the PCG scalars
+// recomputed so that the next direction is z + beta p with the same p.
+template <int DIM>
+__global__ void __launch_bounds__(256) k_ru_rescale(const double* __restrict__ r64, float* __restrict__ r32,
+                                                    float* __restrict__ x32, float* __restrict__ P0,
+                                                    float* __restrict__ P1, const float* __restrict__ dinv,
+                                                    const Modal<float, DIM> M, long long nnodes, double s_old,
+                                                    double s_new, double tol2, PcgState* st, double* partials) {
+    const int it = st->it;                      // the last direction is P[(it - 1) & 1]
+    float* __restrict__ p = ((it - 1) & 1) ? P1 : P0;
+    const double inv = 1.0 / s_new;
+    const float ratio = (float)(s_old / s_new);
+    float arz = 0.f, arr = 0.f;
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < nnodes;
+         n += (long long)gridDim.x * blockDim.x) {
+        const float d = dinv[n];
+#pragma unroll
+        for (int c = 0; c < DIM; ++c) {
+            const long long i = DIM * n + c;
+            const float rn = (float)(r64[i] * inv);
+            r32[i] = rn;
+            x32[i] = 0.f;
+            p[i] *= ratio;
+            arz = fmaf(rn, d * M.kdinv[c] * rn, arz);
+            arr = fmaf(rn, rn, arr);
+        }
+    }
+    double v[2] = {(double)arz, (double)arr}, tot[2];
+    if (grid_reduce_last<2>(v, partials, &st->cnt[1], tot)) {
+        if (threadIdx.x == 0) {
+            const double rz_prev = st->rz_old * (s_old / s_new) * (s_old / s_new);
+            st->rz = tot[0];
+            st->beta = rz_prev > 0.0 ? tot[0] / rz_prev : 0.0;
+            st->rr = tot[1];
+            st->rr_max = tot[1];
+            st->tol2 = tol2;
+            st->status = 0;
+            st->done = (tot[1] <= tol2) ? 1 : 0;
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------
