@@ -84,6 +84,7 @@ struct tog_handle {
     float* d_dinv32 = nullptr;
     double *d_u = nullptr, *d_r64 = nullptr, *d_p64[2] = {nullptr, nullptr}, *d_q64 = nullptr;
     float *d_x32 = nullptr, *d_r32 = nullptr, *d_p32[2] = {nullptr, nullptr}, *d_q32 = nullptr;
+    char* d_vecpool = nullptr;    // backing store of the dof-sized vectors below
     double* d_tmp = nullptr;      // dof-sized staging
     double* d_tmp2 = nullptr;
     double* d_cell[6] = {};       // cell-sized scratch
@@ -123,7 +124,7 @@ struct tog_handle {
     double* d_side64[8] = {};
     // graphs
     cudaGraphExec_t g_pcg64 = nullptr, g_pcg32 = nullptr, g_oc = nullptr;
-    int graph_nodes_pcg = 0;
+    int graph_nodes64 = 0, graph_nodes32 = 0;
 
     Dims dims() const {
         Dims D;
@@ -136,9 +137,9 @@ struct tog_handle {
         D.ncells = ncells;
         return D;
     }
-    int upd_blocks() const {   // PCG update grid: a few blocks per SM, grid-stride over node pairs
-        long long b = (nnodes + 2LL * kEwThreads - 1) / (2LL * kEwThreads);
-        const long long cap = (long long)nsm * 4;
+    int upd_blocks() const {   // PCG update grid: a few blocks per SM, grid-stride over dof groups
+        long long b = (3 * nnodes + 4LL * kEwThreads - 1) / (4LL * kEwThreads);
+        const long long cap = (long long)nsm * 4;   // few blocks: the last-block reduction tail grows with the grid
         return (int)std::max(1LL, std::min(b, cap));
     }
     int ew_blocks(long long n) const {
@@ -157,6 +158,18 @@ int dalloc(T** p, size_t n) {
     cudaError_t e = cudaMalloc((void**)p, n * sizeof(T) + 16);
     if (e != cudaSuccess) return fail(TOG_ERR_OOM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
     return TOG_OK;
+}
+
+// Dof-sized vectors are read together at the same index; their base addresses
+// are staggered by distinct multiples of 1.25 KiB inside one pool so that
+// equal offsets do not land on the same DRAM channel.
+template <typename T>
+T* pool_take(char*& cursor, size_t n, int slot) {
+    const size_t stagger = (size_t)slot * 1280;
+    T* p = reinterpret_cast<T*>(cursor + stagger);
+    const size_t bytes = ((n * sizeof(T) + stagger + 256 + 4095) / 4096) * 4096;
+    cursor += bytes;
+    return p;
 }
 
 dim3 mv3_grid(const tog_handle* h) {
@@ -257,6 +270,7 @@ Mv3Args<T> mv3_args(tog_handle* h) {
     A.LZ = h->LZ;
     A.div_nnx = make_fastdiv((unsigned)h->nn[0]);
     A.div_nny = make_fastdiv((unsigned)h->nn[1]);
+    A.div_nnz = make_fastdiv((unsigned)h->nn[2]);
     for (int c = 0; c < 8; ++c)
         A.side[c] = std::is_same<T, double>::value ? (T*)h->d_side64[c] : (T*)h->d_side32[c];
     return A;
@@ -313,6 +327,14 @@ void launch_pcg_update(tog_handle* h, cudaStream_t s) {
         Mv3Args<T> A = mv3_args<T>(h);
         T* x = std::is_same<T, double>::value ? (T*)h->d_u : (T*)h->d_x32;
         T* r = std::is_same<T, double>::value ? (T*)h->d_r64 : (T*)h->d_r32;
+        const long long n_side = (long long)(h->nt[0] - 1) * h->nn[1] * h->nn[2] +
+                                 (long long)(h->nt[1] - 1) * h->nn[0] * h->nn[2] +
+                                 (long long)(h->nt[2] - 1) * h->nn[0] * h->nn[1];
+        if (n_side > 0) {
+            const long long nbs = std::min<long long>((n_side + kEwThreads - 1) / kEwThreads, (long long)h->nsm * 8);
+            k_side_gather3<T><<<(int)nbs, kEwThreads, 0, s>>>(A);
+            TOG_LAUNCHED(1);
+        }
         k_pcg_update3<T><<<h->upd_blocks(), kEwThreads, 0, s>>>(A, x, r, (T)h->meandiag);
     } else if (std::is_same<T, double>::value) {
             k_pcg_update<double, 2><<<nb, kEwThreads, 0, s>>>(h->d_u, h->d_r64, h->d_p64[0], h->d_p64[1], h->d_q64,
@@ -359,11 +381,15 @@ template <typename T>
 int build_pcg_graph(tog_handle* h, cudaGraphExec_t* out) {
     cudaGraph_t g = nullptr;
     TOG_CUDA(cudaStreamBeginCapture(h->own, cudaStreamCaptureModeThreadLocal));
+    const long long before = g_launches.load();
     for (int i = 0; i < kPcgBatch; ++i) {
         launch_matvec<T, MV_PCG>(h, h->own, nullptr, nullptr, nullptr);
         launch_pcg_update<T>(h, h->own);
     }
-    TOG_LAUNCHED(-2 * kPcgBatch);   // counted when the graph is launched
+    // kernels per batch; captured launches run only when the graph is launched
+    const int nodes = (int)(g_launches.load() - before);
+    g_launches.fetch_sub(nodes);
+    (std::is_same<T, double>::value ? h->graph_nodes64 : h->graph_nodes32) = nodes;
     TOG_CUDA(cudaStreamEndCapture(h->own, &g));
     TOG_CUDA(cudaGraphInstantiate(out, g, 0));
     cudaGraphDestroy(g);
@@ -385,7 +411,7 @@ int run_pcg(tog_handle* h) {
     TOG_TRY(sync_state(h, d_st));
     while (!h->h_st->done) {
         TOG_CUDA(cudaGraphLaunch(*g, h->stream));
-        TOG_LAUNCHED(2 * kPcgBatch);
+        TOG_LAUNCHED((std::is_same<T, double>::value ? h->graph_nodes64 : h->graph_nodes32));
         TOG_TRY(sync_state(h, d_st));
     }
     return TOG_OK;
@@ -806,24 +832,34 @@ int tog_create(const tog_problem_desc* desc, tog_handle** out) {
     A(dalloc(&h->d_int2ref, N));
     A(dalloc(&h->d_ref2int, N));
     A(dalloc(&h->d_fixmask, NN));
-    A(dalloc(&h->d_f, N));
+
     A(dalloc(&h->d_vars, NC));
     A(dalloc(&h->d_e64, NC));
     A(dalloc(&h->d_e32, NC));
     A(dalloc(&h->d_dinv64, NN));
     A(dalloc(&h->d_dinv32, NN));
-    A(dalloc(&h->d_u, N));
-    A(dalloc(&h->d_r64, N));
-    A(dalloc(&h->d_p64[0], N));
-    A(dalloc(&h->d_p64[1], N));
-    A(dalloc(&h->d_q64, N));
-    A(dalloc(&h->d_x32, N));
-    A(dalloc(&h->d_r32, N));
-    A(dalloc(&h->d_p32[0], N));
-    A(dalloc(&h->d_p32[1], N));
-    A(dalloc(&h->d_q32, N));
-    A(dalloc(&h->d_tmp, N));
-    A(dalloc(&h->d_tmp2, N));
+    {   // dof-sized vectors from one pool, base addresses staggered (pool_take)
+        const size_t per64 = ((N * 8 + 13 * 1280 + 256 + 4095) / 4096) * 4096;
+        const size_t per32 = ((N * 4 + 13 * 1280 + 256 + 4095) / 4096) * 4096;
+        A(dalloc(&h->d_vecpool, 8 * per64 + 5 * per32));
+        if (rc == TOG_OK) {
+            char* cur = h->d_vecpool;
+            int slot = 0;
+            h->d_f = pool_take<double>(cur, N, slot++);
+            h->d_u = pool_take<double>(cur, N, slot++);
+            h->d_r64 = pool_take<double>(cur, N, slot++);
+            h->d_p64[0] = pool_take<double>(cur, N, slot++);
+            h->d_p64[1] = pool_take<double>(cur, N, slot++);
+            h->d_q64 = pool_take<double>(cur, N, slot++);
+            h->d_tmp = pool_take<double>(cur, N, slot++);
+            h->d_tmp2 = pool_take<double>(cur, N, slot++);
+            h->d_x32 = pool_take<float>(cur, N, slot++);
+            h->d_r32 = pool_take<float>(cur, N, slot++);
+            h->d_p32[0] = pool_take<float>(cur, N, slot++);
+            h->d_p32[1] = pool_take<float>(cur, N, slot++);
+            h->d_q32 = pool_take<float>(cur, N, slot++);
+        }
+    }
     for (int i = 0; i < 6; ++i) A(dalloc(&h->d_cell[i], NC));
     A(dalloc(&h->d_nodal, NN));
     A(dalloc(&h->d_st64, 1));
@@ -887,11 +923,10 @@ int tog_destroy(tog_handle* h) {
     if (h->g_pcg64) cudaGraphExecDestroy(h->g_pcg64);
     if (h->g_pcg32) cudaGraphExecDestroy(h->g_pcg32);
     if (h->g_oc) cudaGraphExecDestroy(h->g_oc);
-    void* ptrs[] = {h->d_int2ref, h->d_ref2int, h->d_fixmask, h->d_f,   h->d_vars,  h->d_e64,    h->d_e32,
-                    h->d_dinv64,  h->d_dinv32,  h->d_u,       h->d_r64, h->d_p64[0], h->d_p64[1], h->d_q64,
-                    h->d_x32,     h->d_r32,     h->d_p32[0],  h->d_p32[1], h->d_q32, h->d_tmp,    h->d_tmp2,
-                    h->d_nodal,   h->d_st64,    h->d_st32,    h->d_oc,  h->d_partials, h->d_cnt,  h->d_scalar,
-                    h->d_invW,    h->d_soff,    h->d_sw};
+    void* ptrs[] = {h->d_int2ref, h->d_ref2int, h->d_fixmask, h->d_vecpool, h->d_vars,    h->d_e64,
+                    h->d_e32,     h->d_dinv64,  h->d_dinv32,  h->d_nodal,   h->d_st64,    h->d_st32,
+                    h->d_oc,      h->d_partials, h->d_cnt,    h->d_scalar,  h->d_invW,    h->d_soff,
+                    h->d_sw};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (int i = 0; i < 6; ++i)

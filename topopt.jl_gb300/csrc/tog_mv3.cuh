@@ -60,7 +60,7 @@ struct Mv3Args {
     int nn[3];
     int nt[3];             // tiles in x, y, z
     int LZ;                // layers per z chunk
-    FastDiv div_nnx, div_nny;
+    FastDiv div_nnx, div_nny, div_nnz;
     PcgState* st;
     double* partials;
     Modal<T, 3> M;
@@ -531,44 +531,10 @@ __global__ void __launch_bounds__(256) k_mv3_finalize(const Mv3Args<T> A, const 
         if (threadIdx.x == 0) A.st->rr = tot[0];
 }
 
-// PCG update for the 3D operator: q_final from owner + side partials, fixed rows
-// q = meandiag p (= 0), then x += alpha p, r -= alpha q, r.z and r.r partials.
-// Grid-stride over pairs of nodes; all loads of a pair are issued before any use.
-template <typename T>
-__device__ __forceinline__ void upd_node(const Mv3Args<T>& A, const T* __restrict__ p, T* __restrict__ x,
-                                         T* __restrict__ r, T alpha, T meandiag, unsigned n, const T (&qv0)[3],
-                                         const T (&pv)[3], const T (&xv)[3], const T (&rv)[3], unsigned m, T d,
-                                         T& arz, T& arr) {
-    const unsigned row = fdiv(n, A.div_nnx);
-    const int i = (int)(n - row * A.div_nnx.d);
-    const unsigned k_ = fdiv(row, A.div_nny);
-    const int j = (int)(row - k_ * A.div_nny.d), k = (int)k_;
-    T qv[3] = {qv0[0], qv0[1], qv0[2]};
-    const bool fx = (i & 31) == 0 && i > 0 && i < A.nel[0];
-    const bool fy = (j % MV3_BY) == 0 && j > 0 && j < A.nel[1];
-    const bool fz = (k % A.LZ) == 0 && k > 0 && k < A.nel[2];
-    if (fx | fy | fz) {
-#pragma unroll 1
-        for (int cls = 1; cls < 8; ++cls) {
-            const bool on = ((cls & 1) ? fx : true) && ((cls & 2) ? fy : true) && ((cls & 4) ? fz : true);
-            if (on) {
-                const long long s = side_index(A, cls, i, j, k);
-#pragma unroll
-                for (int c = 0; c < 3; ++c) qv[c] += A.side[cls][3 * s + c];
-            }
-        }
-    }
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        const T qq = ((m >> c) & 1u) ? meandiag * pv[c] : qv[c];
-        x[3ull * n + c] = fma(alpha, pv[c], xv[c]);
-        const T rn = fma(-alpha, qq, rv[c]);
-        r[3ull * n + c] = rn;
-        arz = fma(rn, d * A.M.kdinv[c] * rn, arz);
-        arr = fma(rn, rn, arr);
-    }
-}
-
+// PCG update for the 3D operator: fixed rows q = meandiag p (= 0), then
+// x += alpha p, r -= alpha q, r.z and r.r partials.  q already holds K p: the
+// side partials of the tile-boundary nodes were added by k_side_gather3.  The FP32
+// dof arrays are streamed as float4 (4 dofs per thread and step).
 template <typename T>
 __global__ void __launch_bounds__(256) k_pcg_update3(const Mv3Args<T> A, T* __restrict__ x, T* __restrict__ r,
                                                      T meandiag) {
@@ -579,27 +545,66 @@ __global__ void __launch_bounds__(256) k_pcg_update3(const Mv3Args<T> A, T* __re
     const T* __restrict__ q = A.q;
     const T alpha = (T)st->alpha;
     const unsigned nnodes = (unsigned)A.nn[0] * A.nn[1] * A.nn[2];
-    const unsigned stride = gridDim.x * blockDim.x;
+    const unsigned ndofs = 3u * nnodes;
     T arz = T(0), arr = T(0);
-    for (unsigned n0 = blockIdx.x * blockDim.x + threadIdx.x; n0 < nnodes; n0 += 2 * stride) {
-        const unsigned n1 = n0 + stride;
-        const bool has1 = n1 < nnodes;
-        T q0[3], p0[3], x0[3], r0[3], q1[3], p1[3], x1[3], r1[3];
+    if (sizeof(T) == 4) {
+        const unsigned nv = ndofs / 4;   // float4 groups; the tail (< 4 dofs) below
+        const float4* __restrict__ q4 = reinterpret_cast<const float4*>(q);
+        const float4* __restrict__ p4 = reinterpret_cast<const float4*>(p);
+        float4* __restrict__ x4 = reinterpret_cast<float4*>(x);
+        float4* __restrict__ r4 = reinterpret_cast<float4*>(r);
+        for (unsigned g = blockIdx.x * blockDim.x + threadIdx.x; g < nv; g += gridDim.x * blockDim.x) {
+            const float4 qv = q4[g], pv = p4[g], xv = x4[g], rv = r4[g];
+            const float qa[4] = {qv.x, qv.y, qv.z, qv.w};
+            const float pa[4] = {pv.x, pv.y, pv.z, pv.w};
+            const float xa[4] = {xv.x, xv.y, xv.z, xv.w}, ra[4] = {rv.x, rv.y, rv.z, rv.w};
+            float xo[4], ro[4];
+            const unsigned f0 = 4u * g;
+            const unsigned n0 = f0 / 3u;
+            const unsigned c0 = f0 - 3u * n0;
+            const unsigned nb = n0 + 1 < nnodes ? n0 + 1 : n0;
+            const unsigned m0 = A.fixmask[n0], m1 = A.fixmask[nb];
+            const float d0 = (float)A.dinv[n0], d1 = (float)A.dinv[nb];
 #pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            q0[c] = q[3ull * n0 + c];
-            p0[c] = p[3ull * n0 + c];
-            x0[c] = x[3ull * n0 + c];
-            r0[c] = r[3ull * n0 + c];
-            q1[c] = has1 ? q[3ull * n1 + c] : T(0);
-            p1[c] = has1 ? p[3ull * n1 + c] : T(0);
-            x1[c] = has1 ? x[3ull * n1 + c] : T(0);
-            r1[c] = has1 ? r[3ull * n1 + c] : T(0);
+            for (int t = 0; t < 4; ++t) {
+                const unsigned c = c0 + t;              // 0..5: node n0 (c < 3) or n0 + 1
+                const bool second = c >= 3u;
+                const unsigned cc = second ? c - 3u : c;
+                const unsigned m = second ? m1 : m0;
+                const float d = second ? d1 : d0;
+                const float kd = (float)A.M.kdinv[cc];
+                const float qq = ((m >> cc) & 1u) ? (float)meandiag * pa[t] : qa[t];
+                xo[t] = fmaf((float)alpha, pa[t], xa[t]);
+                const float rn = fmaf(-(float)alpha, qq, ra[t]);
+                ro[t] = rn;
+                arz = fmaf(rn, d * kd * rn, arz);
+                arr = fmaf(rn, rn, arr);
+            }
+            x4[g] = make_float4(xo[0], xo[1], xo[2], xo[3]);
+            r4[g] = make_float4(ro[0], ro[1], ro[2], ro[3]);
         }
-        const unsigned m0 = A.fixmask[n0], m1 = has1 ? A.fixmask[n1] : 0u;
-        const T d0 = A.dinv[n0], d1 = has1 ? A.dinv[n1] : T(0);
-        upd_node(A, p, x, r, alpha, meandiag, n0, q0, p0, x0, r0, m0, d0, arz, arr);
-        if (has1) upd_node(A, p, x, r, alpha, meandiag, n1, q1, p1, x1, r1, m1, d1, arz, arr);
+        // tail dofs
+        for (unsigned f = 4u * nv + blockIdx.x * blockDim.x + threadIdx.x; f < ndofs; f += gridDim.x * blockDim.x) {
+            const unsigned n = f / 3u, c = f - 3u * n;
+            const unsigned m = A.fixmask[n];
+            const T qq = ((m >> c) & 1u) ? meandiag * p[f] : q[f];
+            x[f] = fma(alpha, p[f], x[f]);
+            const T rn = fma(-alpha, qq, r[f]);
+            r[f] = rn;
+            arz = fma(rn, A.dinv[n] * A.M.kdinv[c] * rn, arz);
+            arr = fma(rn, rn, arr);
+        }
+    } else {
+        for (unsigned f = blockIdx.x * blockDim.x + threadIdx.x; f < ndofs; f += gridDim.x * blockDim.x) {
+            const unsigned n = f / 3u, c = f - 3u * n;
+            const unsigned m = A.fixmask[n];
+            const T qq = ((m >> c) & 1u) ? meandiag * p[f] : q[f];
+            x[f] = fma(alpha, p[f], x[f]);
+            const T rn = fma(-alpha, qq, r[f]);
+            r[f] = rn;
+            arz = fma(rn, A.dinv[n] * A.M.kdinv[c] * rn, arz);
+            arr = fma(rn, rn, arr);
+        }
     }
     double v[2] = {(double)arz, (double)arr}, tot[2];
     if (grid_reduce_last<2>(v, A.partials, &st->cnt[1], tot)) {
@@ -625,6 +630,61 @@ __global__ void __launch_bounds__(256) k_pcg_update3(const Mv3Args<T> A, T* __re
             }
             st->rr_max = fmax(st->rr_max, tot[1]);
         }
+    }
+}
+
+// Adds the side partials into q at the tile-boundary nodes (x = 32 m, y = 8 m or
+// z = LZ m planes), so that q holds K p before the update streams it.  One
+// thread per boundary node; the three plane families are enumerated without
+// duplicates (a node on several families is visited once, by its lowest family).
+template <typename T>
+__global__ void __launch_bounds__(256) k_side_gather3(const Mv3Args<T> A) {
+    if (A.st->done) return;
+    const int nnx = A.nn[0], nny = A.nn[1], nnz = A.nn[2];
+    const long long tx = A.nt[0] - 1, ty = A.nt[1] - 1, tz = A.nt[2] - 1;
+    const long long cx = tx * nny * nnz;   // family X: i = 32 mx, all j, k
+    const long long cy = ty * nnx * nnz;   // family Y: j = 8 my, i not on an X plane
+    const long long cz = tz * nnx * nny;   // family Z: k = LZ mz, i, j not on X / Y planes
+    const unsigned tot = (unsigned)(cx + cy + cz);
+    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < tot; t += gridDim.x * blockDim.x) {
+        int i, j, k;
+        if (t < (unsigned)cx) {
+            const unsigned a = fdiv(t, A.div_nny), b = fdiv(a, A.div_nnz);
+            j = (int)(t - a * (unsigned)nny);
+            k = (int)(a - b * (unsigned)nnz);
+            i = 32 * (int)(b + 1);
+        } else if (t < (unsigned)(cx + cy)) {
+            const unsigned u = t - (unsigned)cx;
+            const unsigned a = fdiv(u, A.div_nnx), b = fdiv(a, A.div_nnz);
+            i = (int)(u - a * (unsigned)nnx);
+            k = (int)(a - b * (unsigned)nnz);
+            j = MV3_BY * (int)(b + 1);
+            if ((i & 31) == 0 && i > 0 && i < A.nel[0]) continue;
+        } else {
+            const unsigned u = t - (unsigned)(cx + cy);
+            const unsigned a = fdiv(u, A.div_nnx), b = fdiv(a, A.div_nny);
+            i = (int)(u - a * (unsigned)nnx);
+            j = (int)(a - b * (unsigned)nny);
+            k = A.LZ * (int)(b + 1);
+            if ((i & 31) == 0 && i > 0 && i < A.nel[0]) continue;
+            if ((j % MV3_BY) == 0 && j > 0 && j < A.nel[1]) continue;
+        }
+        const bool fx = (i & 31) == 0 && i > 0 && i < A.nel[0];
+        const bool fy = (j % MV3_BY) == 0 && j > 0 && j < A.nel[1];
+        const bool fz = (k % A.LZ) == 0 && k > 0 && k < A.nel[2];
+        const long long n = i + (long long)nnx * (j + (long long)nny * k);
+        T v[3] = {T(0), T(0), T(0)};
+#pragma unroll 1
+        for (int cls = 1; cls < 8; ++cls) {
+            const bool on = ((cls & 1) ? fx : true) && ((cls & 2) ? fy : true) && ((cls & 4) ? fz : true);
+            if (on) {
+                const long long s = side_index(A, cls, i, j, k);
+#pragma unroll
+                for (int c = 0; c < 3; ++c) v[c] += A.side[cls][3 * s + c];
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) A.q[3 * n + c] += v[c];
     }
 }
 
