@@ -165,6 +165,31 @@ int tog_bench_kernel(tog_handle* h, int32_t kernel, int32_t precision, int32_t n
 /* Algorithmic bytes moved by one launch of that kernel. */
 int tog_kernel_bytes(tog_handle* h, int32_t kernel, int32_t precision, double* bytes);
 
+/* ---- batched 2D SIMP (no counterpart in TopOpt.jl: many independent problems at once) --
+ * nprob 2D cantilevers (PointLoadCantilever-style: left edge clamped, unit load [0,-1] at
+ * node (nelx, load_j)), each with its own size, volume fraction and filter radius, sharing
+ * the element size and material of `material` (dim 2).  Every design iteration of all
+ * problems (density filter, FP32-IR solve, compliance, filter pullback, OC) is ONE CUDA
+ * graph launch whose PCG and bisection loops run as device-side conditional nodes. */
+typedef struct tog_batch tog_batch;
+typedef struct tog_batch_stats {
+    int32_t steps;           /* design iterations done */
+    int32_t pcg_loops;       /* PCG iterations of the slowest problem in the last step */
+    int32_t failed;          /* problems whose solve did not converge in the last step */
+    int32_t reserved;
+} tog_batch_stats;
+int tog_batch_create(int32_t nprob, const int32_t* nelx, const int32_t* nely, const int32_t* load_j,
+                     const double* volfrac, const double* rmin, const tog_problem_desc* material, double rtol,
+                     int32_t maxiter, tog_batch** out);
+int tog_batch_destroy(tog_batch* b);
+int tog_batch_set_stream(tog_batch* b, void* stream);
+/* Chooses the operator's chunk height by timing the candidates; re-records the graph. */
+int tog_batch_autotune(tog_batch* b, int32_t* chunk_rows);
+int tog_batch_step(tog_batch* b, tog_batch_stats* stats);
+/* Per-problem compliance, max design change and PCG iterations of the last step (may be NULL). */
+int tog_batch_results(tog_batch* b, double* compliance, double* change, int32_t* cg_iterations);
+int tog_batch_get_design(tog_batch* b, int32_t prob, double* x);
+
 /* ---- allocation-free OC update: no counterpart in TopOpt.jl ----------------------------
  * For callers that cannot call cudaMalloc (a framework that owns and pre-partitions all
  * device memory, a memory-capped service, a loop that must not allocate between

@@ -8,6 +8,7 @@ __graft_entry__.py; the directory name carries a dot).
 """
 from ._lib import TopOptError, NotConverged, lib  # noqa: F401
 from .topopt_api import (  # noqa: F401
+    BatchedSIMP,
     ComplianceFun,
     DensityFilterFun,
     FEASolver,
@@ -21,6 +22,7 @@ from .topopt_api import (  # noqa: F401
     SIMPLoop,
     VolumeFun,
     cell_dofs,
+    config3_problems,
     element_stiffness,
     grid_counts,
     node_dofs,

@@ -26,6 +26,10 @@ class SolveStats(C.Structure):
                 ("reserved", C.c_int32), ("rel_residual", C.c_double), ("abs_residual", C.c_double)]
 
 
+class BatchStats(C.Structure):
+    _fields_ = [("steps", C.c_int32), ("pcg_loops", C.c_int32), ("failed", C.c_int32), ("reserved", C.c_int32)]
+
+
 class IterStats(C.Structure):
     _fields_ = [("compliance", C.c_double), ("volume", C.c_double), ("change", C.c_double),
                 ("lambda_", C.c_double), ("cg_iterations", C.c_int32), ("outer_iterations", C.c_int32),
@@ -68,6 +72,14 @@ SIGNATURES = {
     "tog_get_physical": (C.c_int, [_H, _D]),
     "tog_bench_kernel": (C.c_int, [_H, C.c_int32, C.c_int32, C.c_int32]),
     "tog_kernel_bytes": (C.c_int, [_H, C.c_int32, C.c_int32, _D]),
+    "tog_batch_create": (C.c_int, [C.c_int32, _I32, _I32, _I32, _D, _D, C.POINTER(ProblemDesc), C.c_double, C.c_int32,
+                                   C.POINTER(_H)]),
+    "tog_batch_destroy": (C.c_int, [_H]),
+    "tog_batch_set_stream": (C.c_int, [_H, C.c_void_p]),
+    "tog_batch_autotune": (C.c_int, [_H, _I32]),
+    "tog_batch_step": (C.c_int, [_H, C.POINTER(BatchStats)]),
+    "tog_batch_results": (C.c_int, [_H, _D, _D, _I32]),
+    "tog_batch_get_design": (C.c_int, [_H, C.c_int32, _D]),
     "tog_oc_update_noalloc": (C.c_int, [C.c_int64, _D, _D, _D, _D, C.c_double, C.c_double, _D, _D, C.c_void_p]),
 }
 

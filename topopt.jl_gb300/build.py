@@ -31,6 +31,8 @@ def build(verbose=False):
     jobs = [
         [NVCC] + COMMON + ARCH + ["-lineinfo", "-c", os.path.join(CSRC, "tog_api.cu"),
                                   "-o", os.path.join(BUILD, "tog_api.o")] + (["-Xptxas", "-v"] if verbose else []),
+        [NVCC] + COMMON + ARCH + ["-lineinfo", "-c", os.path.join(CSRC, "tog_batch.cu"),
+                                  "-o", os.path.join(BUILD, "tog_batch.o")],
         [NVCC] + COMMON + ARCH + ["-lineinfo", "-c", os.path.join(CSRC, "tog_noalloc.cu"),
                                   "-o", os.path.join(BUILD, "tog_noalloc.o")],
         [NVCC] + COMMON + ["-x", "c++", "-c", os.path.join(CSRC, "tog_host.cpp"),
@@ -39,7 +41,7 @@ def build(verbose=False):
     with ThreadPoolExecutor(len(jobs)) as ex:
         logs = list(ex.map(_run, jobs))
     tmp = LIB + ".tmp"
-    _run([NVCC] + ARCH + ["-shared", "-o", tmp, os.path.join(BUILD, "tog_api.o"),
+    _run([NVCC] + ARCH + ["-shared", "-o", tmp, os.path.join(BUILD, "tog_api.o"), os.path.join(BUILD, "tog_batch.o"),
                           os.path.join(BUILD, "tog_noalloc.o"), os.path.join(BUILD, "tog_host.o")])
     os.replace(tmp, LIB)
     if verbose:

@@ -33,6 +33,10 @@ struct Modal {
     T kdinv[DIM];   // 1 / Ke(a,a) for component c (identical at every corner)
 };
 
+// Modes of the matrix-free operator kernels: y = K x, the fused PCG direction
+// update + K p + p.q, and the FP64 residual f - K x.
+enum { MV_PLAIN = 0, MV_PCG = 1, MV_RESID = 2 };
+
 // Solver state kept in device memory so that a whole PCG iteration runs
 // without a host round trip.  Written only by the "last block" of a kernel.
 struct PcgState {

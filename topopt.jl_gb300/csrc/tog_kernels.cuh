@@ -15,88 +15,9 @@
 #include <cuda_runtime.h>
 #include "tog_internal.h"
 #include "tog_reduce.cuh"
+#include "tog_device.cuh"
 
 namespace tog {
-
-// ---------------------------------------------------------------------------
-// modal element operator
-// ---------------------------------------------------------------------------
-template <typename T, int NC>
-__device__ __forceinline__ void hadamard_fwd(T (&v)[NC]) {
-#pragma unroll
-    for (int s = 1; s < NC; s <<= 1)
-#pragma unroll
-        for (int i = 0; i < NC; ++i)
-            if (!(i & s)) {
-                T a = v[i], b = v[i + s];
-                v[i] = a + b;
-                v[i + s] = b - a;
-            }
-}
-template <typename T, int NC>
-__device__ __forceinline__ void hadamard_inv(T (&v)[NC]) {
-#pragma unroll
-    for (int s = NC >> 1; s > 0; s >>= 1)
-#pragma unroll
-        for (int i = 0; i < NC; ++i)
-            if (!(i & s)) {
-                T a = v[i], b = v[i + s];
-                v[i] = a - b;
-                v[i + s] = a + b;
-            }
-}
-
-// b = rho * M a   (a, b in modal space; b[.][0] = 0)
-template <typename T, int DIM>
-__device__ __forceinline__ void modal_mul(const Modal<T, DIM>& M, T rho, const T (&a)[DIM][1 << DIM],
-                                          T (&b)[DIM][1 << DIM]) {
-    constexpr int NC = 1 << DIM;
-#pragma unroll
-    for (int c = 0; c < DIM; ++c) b[c][0] = T(0);
-#pragma unroll
-    for (int m = 1; m < NC; ++m)
-#pragma unroll
-        for (int c = 0; c < DIM; ++c) {
-            T acc = M.D[m][c] * a[c][m];
-#pragma unroll
-            for (int d = 0; d < DIM; ++d)
-                if (d != c && (((m >> c) & 1) != ((m >> d) & 1)))
-                    acc = fma(M.O[m][c][d], a[d][m ^ (1 << c) ^ (1 << d)], acc);
-            b[c][m] = rho * acc;
-        }
-}
-
-// u[c][corner] -> y[c][corner] = rho * Ke u
-template <typename T, int DIM>
-__device__ __forceinline__ void element_apply(const Modal<T, DIM>& M, T rho, T (&u)[DIM][1 << DIM]) {
-    constexpr int NC = 1 << DIM;
-#pragma unroll
-    for (int c = 0; c < DIM; ++c) hadamard_fwd<T, NC>(u[c]);
-    T b[DIM][NC];
-    modal_mul<T, DIM>(M, rho, u, b);
-#pragma unroll
-    for (int c = 0; c < DIM; ++c) {
-        hadamard_inv<T, NC>(b[c]);
-#pragma unroll
-        for (int n = 0; n < NC; ++n) u[c][n] = b[c][n];
-    }
-}
-
-// u_e' Ke u_e from corner values (FP64)
-template <int DIM>
-__device__ __forceinline__ double element_energy(const Modal<double, DIM>& M, double (&u)[DIM][1 << DIM]) {
-    constexpr int NC = 1 << DIM;
-#pragma unroll
-    for (int c = 0; c < DIM; ++c) hadamard_fwd<double, NC>(u[c]);
-    double b[DIM][NC];
-    modal_mul<double, DIM>(M, 1.0, u, b);
-    double e = 0.0;
-#pragma unroll
-    for (int c = 0; c < DIM; ++c)
-#pragma unroll
-        for (int m = 1; m < NC; ++m) e = fma(u[c][m], b[c][m], e);
-    return e;
-}
 
 // ---------------------------------------------------------------------------
 // matrix-free operator, 3D hex8: one element column per thread, marching in z.
@@ -109,7 +30,6 @@ constexpr int MV_BY = 8;
 constexpr int MV_LZ = 16;
 constexpr int MV2_WARPS = 4;
 constexpr int MV2_LY = 32;
-enum { MV_PLAIN = 0, MV_PCG = 1, MV_RESID = 2 };
 
 template <typename T, int DIM>
 struct MvArgs {
@@ -578,15 +498,6 @@ __global__ void __launch_bounds__(256) k_ru_rescale(const double* __restrict__ r
 // ---------------------------------------------------------------------------
 // densities -> element scales and the Jacobi diagonal
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double ipow(double x, double p, int ip) {
-    if (ip >= 0) {
-        double r = 1.0;
-        for (int i = 0; i < ip; ++i) r *= x;
-        return r;
-    }
-    return pow(x, p);
-}
-
 __global__ void __launch_bounds__(256) k_escale(const double* __restrict__ vars, double* __restrict__ e64,
                                                 float* __restrict__ e32, long long ncells, double xmin, double p,
                                                 int ip) {
@@ -667,13 +578,6 @@ __global__ void __launch_bounds__(256) k_compliance(const double* __restrict__ u
 // cells; M2: node -> element cone with weight (rmin - d) * valence(node).
 // J = M2 M1 (DensityFilterFun forward, SensFilterFun pullback); J' = M1' M2'.
 // ---------------------------------------------------------------------------
-template <int DIM>
-__device__ __forceinline__ int valence(int ix, int iy, int iz, const Dims& D) {
-    int v = (ix > 0 && ix < D.nel[0] ? 2 : 1) * (iy > 0 && iy < D.nel[1] ? 2 : 1);
-    if (DIM == 3) v *= (iz > 0 && iz < D.nel[2] ? 2 : 1);
-    return v;
-}
-
 template <int DIM>
 __global__ void __launch_bounds__(256) k_filt_node_avg(const double* __restrict__ xe, double* __restrict__ nodal,
                                                        Dims D) {

@@ -365,3 +365,78 @@ class SIMPLoop:
         out = np.empty(self.solver.problem.ncells)
         L.check(L.lib().tog_get_physical(self.solver.handle, L.dptr(out)))
         return out
+
+
+# --------------------------------------------------------------------------- batched 2D
+def config3_problems(n=256, seed=0):
+    """Problem set of the batched benchmark configuration: nelx ~ U{64..512} (even),
+    nely = nelx / 2, the load node uniform on the right edge, volume fraction
+    ~ U[0.3, 0.6], rmin ~ U[1.5, 3.0], from numpy default_rng(seed)."""
+    rng = np.random.default_rng(seed)
+    nelx = 2 * rng.integers(32, 257, size=n)
+    nely = nelx // 2
+    load_j = np.array([rng.integers(0, ny + 1) for ny in nely])
+    volfrac = rng.uniform(0.3, 0.6, size=n)
+    rmin = rng.uniform(1.5, 3.0, size=n)
+    return dict(nelx=nelx, nely=nely, load_j=load_j, volfrac=volfrac, rmin=rmin, seed=seed)
+
+
+class BatchedSIMP:
+    """Many independent 2D cantilevers (left edge clamped, unit load [0, -1] at node
+    (nelx, load_j)), each with its own size, volume fraction and filter radius.
+    One call to step() is one design iteration of every problem: a single CUDA
+    graph launch with device-side PCG and bisection loops (FP32-IR solves with
+    reliable updates, warm-started from the previous iteration)."""
+
+    def __init__(self, nelx, nely, load_j, volfrac, rmin, *, E=1.0, nu=0.3, xmin=1e-9, penalty=3.0, rtol=1e-8,
+                 maxiter=0):
+        self.nprob = len(nelx)
+        self.nelx = np.ascontiguousarray(nelx, dtype=np.int32)
+        self.nely = np.ascontiguousarray(nely, dtype=np.int32)
+        lj = np.ascontiguousarray(load_j, dtype=np.int32)
+        vf = np.ascontiguousarray(volfrac, dtype=np.float64)
+        rm = np.ascontiguousarray(rmin, dtype=np.float64)
+        d = L.ProblemDesc()
+        d.dim = 2
+        d.size[0] = d.size[1] = 1.0
+        d.E, d.nu, d.xmin, d.penalty = float(E), float(nu), float(xmin), float(penalty)
+        h = L.C.c_void_p()
+        L.check(L.lib().tog_batch_create(self.nprob, L.iptr(self.nelx), L.iptr(self.nely), L.iptr(lj), L.dptr(vf),
+                                         L.dptr(rm), L.C.byref(d), float(rtol), int(maxiter), L.C.byref(h)))
+        self.handle = h
+
+    def close(self):
+        if getattr(self, "handle", None):
+            L.lib().tog_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def autotune(self):
+        ly = L.C.c_int32()
+        L.check(L.lib().tog_batch_autotune(self.handle, L.C.byref(ly)))
+        return ly.value
+
+    def set_stream(self, stream_ptr):
+        L.check(L.lib().tog_batch_set_stream(self.handle, L.C.c_void_p(stream_ptr)))
+
+    def step(self):
+        st = L.BatchStats()
+        L.check(L.lib().tog_batch_step(self.handle, L.C.byref(st)))
+        return st
+
+    def results(self):
+        c = np.empty(self.nprob)
+        ch = np.empty(self.nprob)
+        it = np.empty(self.nprob, dtype=np.int32)
+        L.check(L.lib().tog_batch_results(self.handle, L.dptr(c), L.dptr(ch), L.iptr(it)))
+        return c, ch, it
+
+    def design(self, p):
+        x = np.empty(int(self.nelx[p]) * int(self.nely[p]))
+        L.check(L.lib().tog_batch_get_design(self.handle, int(p), L.dptr(x)))
+        return x
