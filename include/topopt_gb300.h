@@ -176,19 +176,35 @@ typedef struct tog_batch_stats {
     int32_t steps;           /* design iterations done */
     int32_t pcg_loops;       /* PCG iterations of the slowest problem in the last step */
     int32_t failed;          /* problems whose solve did not converge in the last step */
-    int32_t reserved;
+    int32_t reliable_updates; /* FP64 true-residual refreshes of all problems in the last step */
 } tog_batch_stats;
 int tog_batch_create(int32_t nprob, const int32_t* nelx, const int32_t* nely, const int32_t* load_j,
                      const double* volfrac, const double* rmin, const tog_problem_desc* material, double rtol,
                      int32_t maxiter, tog_batch** out);
 int tog_batch_destroy(tog_batch* b);
 int tog_batch_set_stream(tog_batch* b, void* stream);
-/* Chooses the operator's chunk height by timing the candidates; re-records the graph. */
-int tog_batch_autotune(tog_batch* b, int32_t* chunk_rows);
+/* Chooses the operator's band height (8, 16, 32 or 64 node rows per work item of 30 node
+ * columns) and the persistent grid of the FP32 operator by timing PCG iterations of all
+ * problems; re-records the graph.  Touches only solver scratch (the design and
+ * displacements are unchanged). */
+int tog_batch_autotune(tog_batch* b, int32_t* tile_rows);
+/* Sets the band height (8, 16, 32 or 64) without timing; re-records the graph. */
+int tog_batch_set_tile_rows(tog_batch* b, int32_t tile_rows);
 int tog_batch_step(tog_batch* b, tog_batch_stats* stats);
 /* Per-problem compliance, max design change and PCG iterations of the last step (may be NULL). */
 int tog_batch_results(tog_batch* b, double* compliance, double* change, int32_t* cg_iterations);
 int tog_batch_get_design(tog_batch* b, int32_t prob, double* x);
+/* Per-problem solve outcome of the last step (arrays may be NULL): FP64 residual norm
+ * ||f - K u|| at the last refresh, reliable updates (refreshes), status (TOG_OK converged,
+ * TOG_NOT_CONVERGED failed). */
+int tog_batch_solve_info(tog_batch* b, double* residual, int32_t* refreshes, int32_t* status);
+/* Measurement hooks: launch one loop kernel nlaunch times over ALL problems (after the
+ * set-up kernels of a design iteration, outside the graph; only solver scratch changes)
+ * and return the mean microseconds per launch.  kernel 0 = FP32 operator, 1 = PCG vector
+ * update, 2 = FP64 true residual, 3 = operator + update (one PCG loop). */
+int tog_batch_bench_kernel(tog_batch* b, int32_t kernel, int32_t nlaunch, double* us_per_launch);
+/* Algorithmic HBM bytes of one launch of that kernel over all problems. */
+int tog_batch_kernel_bytes(tog_batch* b, int32_t kernel, double* bytes);
 
 /* ---- allocation-free OC update: no counterpart in TopOpt.jl ----------------------------
  * For callers that cannot call cudaMalloc (a framework that owns and pre-partitions all

@@ -20,7 +20,7 @@ def single_run(tg, nelx, nely, volfrac, rmin, steps, rtol):
     return np.array(comps), x
 
 
-@pytest.mark.parametrize("autotune", [False, True])
+@pytest.mark.parametrize("autotune", [False, True, 8, 16, 64])
 def test_batch_matches_single_problems(tg, autotune):
     nelx = [64, 30, 96, 48]
     nely = [32, 16, 20, 48]
@@ -29,8 +29,10 @@ def test_batch_matches_single_problems(tg, autotune):
     lj = [n // 2 for n in nely]
     rtol, steps = 1e-10, 3
     b = tg.BatchedSIMP(nelx, nely, lj, vf, rm, rtol=rtol)
-    if autotune:
-        assert b.autotune() in (8, 16, 32, 64, 128)
+    if autotune is True:
+        assert b.autotune() in (8, 16, 32, 64)
+    elif autotune:
+        b.set_tile_rows(autotune)
     comps = []
     for _ in range(steps):
         st = b.step()
@@ -71,3 +73,22 @@ def test_batch_rejects_bad_problems(tg):
         tg.BatchedSIMP([10], [5], [9], [0.5], [2.0])       # load node beyond the edge
     with pytest.raises(tg.TopOptError):
         tg.BatchedSIMP([10], [6], [3], [0.5], [0.1])       # rmin below the element size
+
+
+@pytest.mark.parametrize("rows", [8, 16, 64])
+def test_batch_tile_rows_same_results(tg, rows):
+    """Every tile height gives the same design iteration on problems that span
+    many tiles; compliance agrees to the solve tolerance."""
+    P = tg.config3_problems(8, seed=3)
+    out = []
+    for r in (rows, None):
+        b = tg.BatchedSIMP(P["nelx"], P["nely"], P["load_j"], P["volfrac"], P["rmin"], rtol=1e-8)
+        if r:
+            b.set_tile_rows(r)
+        st = b.step()
+        assert st.failed == 0
+        res, nref, status = b.solve_info()
+        assert np.all(status == 0) and np.all(res <= 1e-8)
+        out.append(b.results()[0])
+        b.close()
+    assert np.max(np.abs(out[0] - out[1]) / out[1]) < 1e-6

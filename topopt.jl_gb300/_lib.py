@@ -27,7 +27,7 @@ class SolveStats(C.Structure):
 
 
 class BatchStats(C.Structure):
-    _fields_ = [("steps", C.c_int32), ("pcg_loops", C.c_int32), ("failed", C.c_int32), ("reserved", C.c_int32)]
+    _fields_ = [("steps", C.c_int32), ("pcg_loops", C.c_int32), ("failed", C.c_int32), ("reliable_updates", C.c_int32)]
 
 
 class IterStats(C.Structure):
@@ -77,9 +77,13 @@ SIGNATURES = {
     "tog_batch_destroy": (C.c_int, [_H]),
     "tog_batch_set_stream": (C.c_int, [_H, C.c_void_p]),
     "tog_batch_autotune": (C.c_int, [_H, _I32]),
+    "tog_batch_set_tile_rows": (C.c_int, [_H, C.c_int32]),
     "tog_batch_step": (C.c_int, [_H, C.POINTER(BatchStats)]),
     "tog_batch_results": (C.c_int, [_H, _D, _D, _I32]),
     "tog_batch_get_design": (C.c_int, [_H, C.c_int32, _D]),
+    "tog_batch_solve_info": (C.c_int, [_H, _D, _I32, _I32]),
+    "tog_batch_bench_kernel": (C.c_int, [_H, C.c_int32, C.c_int32, C.POINTER(C.c_double)]),
+    "tog_batch_kernel_bytes": (C.c_int, [_H, C.c_int32, C.POINTER(C.c_double)]),
     "tog_oc_update_noalloc": (C.c_int, [C.c_int64, _D, _D, _D, _D, C.c_double, C.c_double, _D, _D, C.c_void_p]),
 }
 

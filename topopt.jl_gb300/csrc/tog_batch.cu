@@ -34,7 +34,6 @@ namespace {
 constexpr int kBThreads = 256;
 constexpr int kNodeChunk = 1024;   // nodes per node item
 constexpr int kCellChunk = 1024;   // cells per cell item
-constexpr int kMvWarps = 4;        // matvec items (warps) per block
 constexpr int kOcMax = 100;        // bisection step cap
 constexpr int kMaxLoops = 1 << 20; // PCG loop cap of one design iteration
 
@@ -43,7 +42,7 @@ enum { M_PCG = 0, M_RU = 1, M_DONE = 2, M_FAIL = 3, M_INIT = 4 };
 struct BProb {
     int nel[2], nn[2];
     long long noff, eoff;        // first node / cell of the problem
-    int mv0, nmv;                // matvec items
+    int t0, nt, ntx, pad;        // operator items (strip x band): first, count, strips along x
     int nd0, nnd;                // node items
     int ce0, nce;                // cell items
     int s0, S;                   // filter stencil slice
@@ -63,6 +62,14 @@ struct BState {
 struct BGlobal {
     unsigned cnt[8];
     int loops, active, failed, oc_active;
+    int list_n[2], updates, pad; // listed problems per work list; reliable updates of the step
+};
+
+enum { kActive = 0, kRefresh = 1 };
+constexpr int kListCache = 1024;   // work-list entries a block keeps in shared memory
+
+struct WList {   // a work list (see the kernels' comments)
+    int *prob, *tpref, *npref;
 };
 
 struct Item {   // one work item
@@ -74,10 +81,12 @@ struct BArgs {
     const BProb* P;
     BState* B;
     BGlobal* G;
-    const Item* mv;
     const Item* nd;
     const Item* ce;
-    int nmv, nnd, nce, nprob, LY;
+    int nnd, nce, nprob, LY;
+    int in_graph;               // kernels set graph conditions only inside the graph
+    int in_loop;                // ... and the refresh condition only inside the PCG loop body
+    WList lst[2];
     const uint8_t* fixmask;
     const double* f;
     double *u, *r64;
@@ -88,9 +97,10 @@ struct BArgs {
     double* partials;           // one slot per item (x2)
     Modal<float, 2> Mf;
     Modal<double, 2> Md;
+    float Kc[2][4][2][4];       // element stiffness by [c][corner][d][corner] (FP32 gather operator)
     double xmin, pen, ru_delta2, move;
     int ip, maxit;
-    cudaGraphConditionalHandle h_pcg, h_oc;
+    cudaGraphConditionalHandle h_pcg, h_oc, h_ru;
 };
 
 // ---- per-problem reduction: partial per item, last item of the problem sums in order
@@ -184,8 +194,10 @@ __device__ __forceinline__ Dims pdims(const BProb& P) {
     return D;
 }
 
+__device__ int build_list(const BArgs& A, int l, int* failed);
+
 // ---------------------------------------------------------------------------
-// design iteration start: every problem to M_INIT, counters cleared
+// design iteration start: every problem to M_INIT, counters cleared, all listed
 __global__ void bk_begin(BArgs A) {
     for (int b = threadIdx.x; b < A.nprob; b += blockDim.x) {
         A.B[b].mode = M_INIT;
@@ -196,7 +208,10 @@ __global__ void bk_begin(BArgs A) {
     if (threadIdx.x == 0) {
         A.G->loops = 0;
         A.G->failed = 0;
+        A.G->updates = 0;
     }
+    __syncthreads();
+    build_list(A, kRefresh, nullptr);   // every problem starts with an FP64 residual
 }
 
 // ---- filters (per problem, node-based, as the single-problem kernels) ----
@@ -332,164 +347,449 @@ __global__ void __launch_bounds__(kBThreads) bk_nodesum(BArgs A) {
 }
 
 // ---------------------------------------------------------------------------
-// matrix-free operator over matvec items: one warp = 32 element columns (31
-// owned node columns) of one problem, marching LY element rows in y.
-//   MV_PCG (FP32): p = D^-1 r + beta p_old, q = K p, p.q -> alpha  (mode M_PCG)
-//   MV_RESID (FP64): r64 = f - K (u + s x32), ||r64||^2 -> decision (modes M_INIT / M_RU)
-template <typename T, int MODE>
-__global__ void __launch_bounds__(32 * kMvWarps) bk_matvec(BArgs A) {
+// Work lists.  The PCG-loop kernels run persistent grids that stride over the
+// tiles (or node chunks) of listed problems only, so finished problems cost
+// nothing in later loops:
+//   list kActive:  problems in PCG mode (rebuilt after every refresh pass)
+//   list kRefresh: problems needing the FP64 true residual (M_INIT or M_RU)
+// List l holds, for its k-th problem (ascending ids): prob[k], the first tile of
+// that problem in the flattened tile range (tpref[k], prefix sum, tpref[n] = total)
+// and its first node chunk (npref[k]); n = G->list_n[l].  Blocks copy a list of up
+// to CAP problems to shared memory and search it there.
+__device__ __forceinline__ int ld_mode(const BState* B, int p) {
+    return *(volatile const int*)&B[p].mode;
+}
+
+// block-wide exclusive scan of three counters; returns the block totals in tot[]
+__device__ __forceinline__ void block_scan3(int (&v)[3], int (&tot)[3]) {
+    __shared__ int sw[3][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    int inc[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        inc[i] = v[i];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, inc[i], o);
+            if (lane >= o) inc[i] += t;
+        }
+        if (lane == 31) sw[i][warp] = inc[i];
+    }
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            int x = lane < nw ? sw[i][lane] : 0;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += t;
+            }
+            sw[i][lane] = x;   // inclusive prefix of the warp totals
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const int before = warp > 0 ? sw[i][warp - 1] : 0;
+        tot[i] = sw[i][nw - 1];
+        v[i] = before + inc[i] - v[i];
+    }
+    __syncthreads();
+}
+
+// Rebuild list l from the problem modes (all threads of ONE block, no other
+// kernel running).  Returns the number listed; *failed (thread 0) = failed problems.
+__device__ int build_list(const BArgs& A, int l, int* failed) {
+    __shared__ int s_fail;
+    if (threadIdx.x == 0) s_fail = 0;
+    __syncthreads();
+    const WList& W = A.lst[l];
+    int bk = 0, bt = 0, bn = 0, nf = 0;
+    for (int b0 = 0; b0 < A.nprob; b0 += blockDim.x) {
+        const int p = b0 + threadIdx.x;
+        int v[3] = {0, 0, 0};
+        if (p < A.nprob) {
+            const int m = ld_mode(A.B, p);
+            if (l == kActive ? (m == M_PCG) : (m == M_INIT || m == M_RU)) {
+                v[0] = 1;
+                v[1] = A.P[p].nt;
+                v[2] = A.P[p].nnd;
+            }
+            nf += (m == M_FAIL);
+        }
+        const int flag = v[0];
+        int tot[3];
+        block_scan3(v, tot);
+        if (flag) {
+            W.prob[bk + v[0]] = p;
+            W.tpref[bk + v[0]] = bt + v[1];
+            W.npref[bk + v[0]] = bn + v[2];
+        }
+        bk += tot[0];
+        bt += tot[1];
+        bn += tot[2];
+    }
+    if (nf) atomicAdd(&s_fail, nf);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        W.tpref[bk] = bt;
+        W.npref[bk] = bn;
+        A.G->list_n[l] = bk;
+        __threadfence();
+        if (failed) *failed = s_fail;
+    }
+    return bk;
+}
+
+struct ListView {
+    const int* pref;
+    const int* prob;
+    int n, total;
+};
+
+template <bool TILES, int CAP>
+__device__ __forceinline__ ListView load_list(const BArgs& A, int l, int* s_pref, int* s_prob) {
+    const WList& W = A.lst[l];
+    const int* gpref = TILES ? W.tpref : W.npref;
+    ListView V;
+    V.n = __ldcg(&A.G->list_n[l]);
+    V.total = V.n > 0 ? __ldcg(gpref + V.n) : 0;
+    V.pref = gpref;
+    V.prob = W.prob;
+    if (CAP > 0 && V.n > 0 && V.n <= CAP && V.total > (int)blockIdx.x) {
+        for (int i = threadIdx.x; i <= V.n; i += blockDim.x) s_pref[i] = __ldcg(gpref + i);
+        for (int i = threadIdx.x; i < V.n; i += blockDim.x) s_prob[i] = __ldcg(W.prob + i);
+        __syncthreads();
+        V.pref = s_pref;
+        V.prob = s_prob;
+    }
+    return V;
+}
+
+// largest k in [0, n) with pref[k] <= w  (pref ascending, pref[0] = 0 <= w)
+__device__ __forceinline__ int find_seg(const int* pref, int n, int w) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (pref[mid] <= w)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
+// Skip the rest of a listed problem ending at `end`: the loop increment then
+// takes this block's stride past it.
+__device__ __forceinline__ int skip_to(int w, int end) {
+    const int G = gridDim.x;
+    return w + ((end - w + G - 1) / G - 1) * G;
+}
+
+__device__ __forceinline__ void request_refresh(const BArgs& A) {
+    if (A.in_loop) cudaGraphSetConditional(A.h_ru, 1u);
+}
+
+// ---------------------------------------------------------------------------
+// Segmented reduction of the persistent loop kernels.  A block owns a
+// contiguous range of work items (tiles or node chunks of the flattened list)
+// and keeps its partial sums for one problem across consecutive items; at the
+// end of the problem's items in its range it publishes them in the slot of the
+// segment's first item (zeros in the other slots of the segment).  The block
+// that completes a problem's item count sums the problem's slots in order, so
+// the totals do not depend on timing.  Returns true in that block (tot[] set).
+template <int NV>
+__device__ bool seg_flush(double (&v)[NV], double* partials, int seg0, int wend, int pbeg, int pend,
+                          unsigned* counter, double (&tot)[NV]) {
+    __shared__ double sred[NV][32];
+    __shared__ int amlast;
+    block_reduce<NV, false>(v, sred);
+    if (threadIdx.x < 32) {
+        for (int i = seg0 + 1 + (int)threadIdx.x; i < wend; i += 32)
+#pragma unroll
+            for (int j = 0; j < NV; ++j) partials[(size_t)i * NV + j] = 0.0;
+        if (threadIdx.x == 0)
+#pragma unroll
+            for (int j = 0; j < NV; ++j) partials[(size_t)seg0 * NV + j] = v[j];
+        __threadfence();
+        __syncwarp();
+        if (threadIdx.x == 0) {
+            const unsigned n = (unsigned)(wend - seg0);
+            amlast = (atomicAdd(counter, n) + n == (unsigned)(pend - pbeg));
+        }
+    }
+    __syncthreads();
+    if (!amlast) return false;
+    __threadfence();
+    double s[NV];
+#pragma unroll
+    for (int j = 0; j < NV; ++j) s[j] = 0.0;
+    for (int i = pbeg + (int)threadIdx.x; i < pend; i += blockDim.x)
+#pragma unroll
+        for (int j = 0; j < NV; ++j) s[j] += __ldcg(partials + (size_t)i * NV + j);
+    block_reduce<NV, false>(s, sred);
+#pragma unroll
+    for (int j = 0; j < NV; ++j) tot[j] = s[j];
+    if (threadIdx.x == 0) *counter = 0u;
+    return true;
+}
+
+// contiguous item range [w0, w1) of this block
+__device__ __forceinline__ void block_range(int total, int& w0, int& w1) {
+    w0 = (int)((long long)total * blockIdx.x / gridDim.x);
+    w1 = (int)((long long)total * (blockIdx.x + 1) / gridDim.x);
+}
+
+// ---------------------------------------------------------------------------
+// Matrix-free operator as a warp march.  A work item is a strip of 32 node
+// columns (lanes; x = 30 cx - 1 + lane, lanes 1..30 own their column, lanes 0
+// and 31 are halo) by a band of LY node rows of one problem.  The warp walks
+// the node rows of the band (plus one above and one below); lane l applies the
+// element to its upper right in modal form, its corner forces reach the nodes
+// through warp shuffles (columns) and a register carry (rows).  The raw inputs
+// of the next D rows are loaded ahead into a register ring, so each warp keeps
+// D rows of loads in flight with no shared memory and no barriers.
+//   MV_PCG (FP32):   p = D^-1 r + beta p_old, q = K p, p.q -> alpha   (list kActive)
+//   MV_RESID (FP64): v = u + s x32 (fixed dofs zero), r64 = f - K v,
+//                    ||r64||^2 -> refresh decision                   (list kRefresh)
+// Warps own contiguous item ranges; partial sums are flushed per problem
+// segment (slot of the segment's first item, zeros in the rest), and the warp
+// completing a problem sums its slots in order.
+template <int NV>
+__device__ bool warp_seg_flush(double (&v)[NV], double* partials, int seg0, int wend, int pbeg, int pend,
+                               unsigned* counter, double (&tot)[NV]) {
     const int lane = threadIdx.x & 31;
-    const int item = blockIdx.x * kMvWarps + (threadIdx.x >> 5);
-    if (item >= A.nmv) return;
-    const Item it = A.mv[item];
-    const BProb P = A.P[it.prob];
-    BState& S = A.B[it.prob];
-    const int mode = S.mode;
-    if (MODE == MV_PCG && mode != M_PCG) return;
-    if (MODE == MV_RESID && mode != M_INIT && mode != M_RU) return;
-    const int nelx = P.nel[0], nely = P.nel[1], nnx = P.nn[0], nny = P.nn[1];
-    const int ex = 31 * it.a - 1 + lane;
-    const int ky0 = it.b;
-    const bool own_x = lane >= 1 && ex < nnx;
-    T beta = T(0);
-    const float* pold = nullptr;
-    float* pnew = nullptr;
-    double sc = 0.0;
-    if (MODE == MV_PCG) {
-        const int itn = S.pcg.it;
-        pnew = (itn & 1) ? A.P1 : A.P0;
-        pold = (itn & 1) ? A.P0 : A.P1;
-        beta = (T)S.pcg.beta;
-    } else {
-        sc = (mode == M_RU) ? S.s : 0.0;
+#pragma unroll
+    for (int j = 0; j < NV; ++j) v[j] = warp_sum(v[j]);
+    for (int i = seg0 + 1 + lane; i < wend; i += 32)
+#pragma unroll
+        for (int j = 0; j < NV; ++j) partials[(size_t)i * NV + j] = 0.0;
+    if (lane == 0)
+#pragma unroll
+        for (int j = 0; j < NV; ++j) partials[(size_t)seg0 * NV + j] = v[j];
+    __threadfence();
+    __syncwarp();
+    unsigned last = 0;
+    if (lane == 0) {
+        const unsigned n = (unsigned)(wend - seg0);
+        last = (atomicAdd(counter, n) + n == (unsigned)(pend - pbeg)) ? 1u : 0u;
     }
-    const Modal<T, 2>& M = *reinterpret_cast<const Modal<T, 2>*>(sizeof(T) == 4 ? (const void*)&A.Mf : (const void*)&A.Md);
-    auto load_row = [&](int kk, T (&v)[2][2]) {
+    last = __shfl_sync(0xffffffffu, last, 0);
+    if (!last) return false;
+    __threadfence();
+    double s[NV];
 #pragma unroll
-        for (int bx = 0; bx < 2; ++bx) {
-            const int ix = ex + bx;
-            v[0][bx] = v[1][bx] = T(0);
-            if (ix >= 0 && ix < nnx && kk >= 0 && kk < nny) {
-                const long long n = P.noff + ix + (long long)nnx * kk;
-                if (MODE == MV_PCG) {
-                    const float d = A.dinv32[n];
+    for (int j = 0; j < NV; ++j) s[j] = 0.0;
+    for (int i = pbeg + lane; i < pend; i += 32)
 #pragma unroll
-                    for (int c = 0; c < 2; ++c)
-                        v[c][bx] = (T)fmaf((float)beta, pold[2 * n + c], d * A.Mf.kdinv[c] * A.r32[2 * n + c]);
-                } else {
-                    const unsigned m = A.fixmask[n];
+        for (int j = 0; j < NV; ++j) s[j] += __ldcg(partials + (size_t)i * NV + j);
 #pragma unroll
-                    for (int c = 0; c < 2; ++c)
-                        v[c][bx] = ((m >> c) & 1u) ? T(0) : (T)(A.u[2 * n + c] + sc * (double)A.x32[2 * n + c]);
-                }
-            }
-        }
-    };
-    T lo[2][2], up[2][2];
-    load_row(ky0 - 1, lo);
-    T carry[2] = {T(0), T(0)};
-    double acc = 0.0;
-    const int kend = min(ky0 + A.LY - 1, nely);
-    for (int k = ky0 - 1; k <= kend; ++k) {
-        load_row(k + 1, up);
-        T y[2][4];
-        const bool inel = ex >= 0 && ex < nelx && k >= 0 && k < nely;
-        if (inel) {
-            const T rho = (T)(sizeof(T) == 4 ? (double)A.e32[P.eoff + ex + (long long)nelx * k]
-                                             : A.e64[P.eoff + ex + (long long)nelx * k]);
-#pragma unroll
-            for (int c = 0; c < 2; ++c) {
-                y[c][0] = lo[c][0];
-                y[c][1] = lo[c][1];
-                y[c][2] = up[c][0];
-                y[c][3] = up[c][1];
-            }
-            element_apply<T, 2>(M, rho, y);
+    for (int j = 0; j < NV; ++j) tot[j] = warp_sum(s[j]);
+    if (lane == 0) *counter = 0u;
+    return true;
+}
+
+template <typename T, int MODE>
+struct MarchRow;
+template <>
+struct MarchRow<float, MV_PCG> {   // raw inputs of node row j (and element / mask of row j - 1)
+    float2 r, po;
+    float d, rho;
+    unsigned m;
+};
+template <>
+struct MarchRow<double, MV_RESID> {
+    double2 u, f;
+    float2 xs;
+    double rho;
+    unsigned mj;   // fixed mask of row j (zeroes v)
+};
+
+constexpr int kMarchWarps = 8;   // warps per block
+
+template <typename T, int MODE>
+__global__ void __launch_bounds__(32 * kMarchWarps) bk_march(BArgs A) {
+    constexpr int D = (MODE == MV_PCG) ? 4 : 2;   // rows loaded ahead
+    using Row = MarchRow<T, MODE>;
+    using Acc = typename std::conditional<MODE == MV_PCG, float, double>::type;
+    using V2 = typename std::conditional<MODE == MV_PCG, float2, double2>::type;
+    __shared__ int s_pref[kListCache + 1], s_prob[kListCache];
+    if (MODE == MV_PCG && blockIdx.x == 0 && threadIdx.x == 0) A.G->loops += 1;
+    const ListView V = load_list<true, kListCache>(A, MODE == MV_PCG ? kActive : kRefresh, s_pref, s_prob);
+    const int lane = threadIdx.x & 31;
+    const int GW = gridDim.x * kMarchWarps;
+    const int gw = blockIdx.x * kMarchWarps + (threadIdx.x >> 5);
+    const int w0 = (int)((long long)V.total * gw / GW), w1 = (int)((long long)V.total * (gw + 1) / GW);
+    if (w0 >= w1) return;
+    const Modal<T, 2>& M = *reinterpret_cast<const Modal<T, 2>*>(MODE == MV_PCG ? (const void*)&A.Mf : (const void*)&A.Md);
+    const int LY = A.LY;
+    int k = find_seg(V.pref, V.n, w0);
+    int kbeg = V.pref[k], kend = V.pref[k + 1];
+    int seg0 = w0;
+    Acc acc = Acc(0);
+    for (int w = w0; w < w1; ++w) {
+        const int p = V.prob[k];
+        const BProb& P = A.P[p];
+        BState& S = A.B[p];
+        const int nnx = P.nn[0], nny = P.nn[1], nelx = P.nel[0], nely = P.nel[1];
+        const int t = w - kbeg;
+        const int band = t / P.ntx, cx = t - band * P.ntx;
+        const int b0 = band * LY, b1 = min(b0 + LY, nny);
+        const int x = 30 * cx - 1 + lane;
+        const bool colok = x >= 0 && x < nnx;
+        const bool elok = x >= 0 && x < nelx && lane < 31;
+        const bool own = colok && lane >= 1 && lane <= 30;
+        const long long nb = P.noff + x, eb = P.eoff + x;
+        // per-item scalars and row loader
+        T beta = T(0), sc = T(0);
+        int odd = 0, mode = 0;
+        if (MODE == MV_PCG) {
+            beta = (T)S.pcg.beta;
+            odd = S.pcg.it & 1;
         } else {
-#pragma unroll
-            for (int c = 0; c < 2; ++c)
-#pragma unroll
-                for (int j = 0; j < 4; ++j) y[c][j] = T(0);
+            mode = S.mode;
+            sc = (mode == M_RU) ? (T)S.s : T(0);
         }
-        T col[2][2];
-#pragma unroll
-        for (int by = 0; by < 2; ++by)
-#pragma unroll
-            for (int c = 0; c < 2; ++c) {
-                const T t = __shfl_up_sync(0xffffffffu, y[c][1 + 2 * by], 1);
-                col[c][by] = y[c][2 * by] + (lane > 0 ? t : T(0));
-            }
-        if (k >= ky0 && own_x && k < nny) {
-            const long long n = P.noff + ex + (long long)nnx * k;
-            const unsigned m = A.fixmask[n];
-#pragma unroll
-            for (int c = 0; c < 2; ++c) {
-                const T tot = carry[c] + col[c][0];
-                if (MODE == MV_PCG) {
-                    const T pv = lo[c][0];
-                    const T qv = ((m >> c) & 1u) ? T(0) : tot;
-                    pnew[2 * n + c] = (float)pv;
-                    A.q32[2 * n + c] = (float)qv;
-                    acc += (double)pv * (double)qv;
-                } else {
-                    const double rv = ((m >> c) & 1u) ? 0.0 : A.f[2 * n + c] - (double)tot;
-                    A.r64[2 * n + c] = rv;
-                    acc += rv * rv;
-                }
-            }
-        }
-#pragma unroll
-        for (int c = 0; c < 2; ++c) {
-            carry[c] = col[c][1];
-            lo[c][0] = up[c][0];
-            lo[c][1] = up[c][1];
-        }
-    }
-    double v[1] = {acc}, tot[1];
-    if (prob_reduce_warp<1>(v, A.partials, item, P.mv0, P.nmv, &S.cnt[MODE == MV_PCG ? 0 : 1], tot)) {
-        if (lane == 0) {
-            if (MODE == MV_PCG) {
-                S.pcg.pq = tot[0];
-                if (!(tot[0] > 0.0) || !isfinite(tot[0]))
-                    S.mode = M_RU;   // breakdown: refresh from the true residual
-                else
-                    S.pcg.alpha = S.pcg.rz / tot[0];
+        auto load = [&](int j, Row& R) {
+            const bool rok = colok && j >= 0 && j < nny;
+            const long long n = nb + (long long)nnx * j;
+            const bool eok = elok && j >= 1 && j - 1 < nely;
+            const long long e = eb + (long long)nelx * (j - 1);
+            if constexpr (MODE == MV_PCG) {
+                const float2* pold = reinterpret_cast<const float2*>(odd ? A.P0 : A.P1);
+                R.r = rok ? reinterpret_cast<const float2*>(A.r32)[n] : make_float2(0.f, 0.f);
+                R.po = rok ? pold[n] : make_float2(0.f, 0.f);
+                R.d = rok ? A.dinv32[n] : 0.f;
+                R.rho = eok ? A.e32[e] : 0.f;
+                R.m = (own && j >= 1) ? (unsigned)A.fixmask[n - nnx] : 0u;
             } else {
-                const double res = sqrt(tot[0]);
-                S.res = res;
-                if (!isfinite(res)) {
-                    S.mode = M_FAIL;
-                } else if (res <= P.tol) {
-                    S.mode = (mode == M_RU) ? M_RU : M_DONE;   // M_RU: the rescale pass applies the last correction
-                    S.stall = -1;                                // converged marker for the rescale pass
-                } else if (mode == M_RU) {
-                    if (res < 0.5 * S.best) {
-                        S.best = res;
-                        S.stall = 0;
-                    } else if (++S.stall >= 8) {
-                        S.mode = M_FAIL;
+                R.u = rok ? reinterpret_cast<const double2*>(A.u)[n] : make_double2(0.0, 0.0);
+                R.xs = rok ? reinterpret_cast<const float2*>(A.x32)[n] : make_float2(0.f, 0.f);
+                R.mj = rok ? (unsigned)A.fixmask[n] : 0u;
+                R.rho = eok ? A.e64[e] : 0.0;
+                R.f = (own && j >= 1) ? reinterpret_cast<const double2*>(A.f)[n - nnx] : make_double2(0.0, 0.0);
+            }
+        };
+        const int j0 = b0 - 1, j1 = b1;   // node rows walked (inclusive)
+        Row buf[D];
+#pragma unroll
+        for (int s = 0; s < D; ++s)
+            if (j0 + s <= j1) load(j0 + s, buf[s]);
+        V2 plo{}, plr{}, carry{};
+        unsigned mprev = 0;   // fixed mask of row j - 1 (residual mode)
+        for (int jb = j0; jb <= j1; jb += D) {
+#pragma unroll
+            for (int s = 0; s < D; ++s) {
+                const int j = jb + s;
+                if (j > j1) break;
+                const Row R = buf[s];
+                if (j + D <= j1) load(j + D, buf[s]);
+                V2 pj;
+                if constexpr (MODE == MV_PCG) {
+                    pj.x = fmaf(beta, R.po.x, R.d * M.kdinv[0] * R.r.x);
+                    pj.y = fmaf(beta, R.po.y, R.d * M.kdinv[1] * R.r.y);
+                } else {
+                    pj.x = (R.mj & 1u) ? 0.0 : fma(sc, (double)R.xs.x, R.u.x);
+                    pj.y = (R.mj & 2u) ? 0.0 : fma(sc, (double)R.xs.y, R.u.y);
+                }
+                V2 pr;
+                pr.x = __shfl_down_sync(0xffffffffu, pj.x, 1);
+                pr.y = __shfl_down_sync(0xffffffffu, pj.y, 1);
+                if (j >= b0) {   // element row j - 1: corners (lo, lo right, up, up right)
+                    T y[2][4] = {{plo.x, plr.x, pj.x, pr.x}, {plo.y, plr.y, pj.y, pr.y}};
+                    element_apply<T, 2>(M, (T)R.rho, y);
+                    const T t1x = __shfl_up_sync(0xffffffffu, y[0][1], 1);
+                    const T t1y = __shfl_up_sync(0xffffffffu, y[1][1], 1);
+                    const T t3x = __shfl_up_sync(0xffffffffu, y[0][3], 1);
+                    const T t3y = __shfl_up_sync(0xffffffffu, y[1][3], 1);
+                    if (j > b0 && own) {   // node row j - 1 is complete
+                        const T qx = carry.x + y[0][0] + t1x, qy = carry.y + y[1][0] + t1y;
+                        const long long n = nb + (long long)nnx * (j - 1);
+                        if constexpr (MODE == MV_PCG) {
+                            const float2 qv = make_float2((R.m & 1u) ? 0.f : qx, (R.m & 2u) ? 0.f : qy);
+                            reinterpret_cast<float2*>(odd ? A.P1 : A.P0)[n] = plo;
+                            reinterpret_cast<float2*>(A.q32)[n] = qv;
+                            acc = fmaf(plo.x, qv.x, fmaf(plo.y, qv.y, acc));
+                        } else {
+                            const double r0 = (mprev & 1u) ? 0.0 : R.f.x - qx;
+                            const double r1 = (mprev & 2u) ? 0.0 : R.f.y - qy;
+                            reinterpret_cast<double2*>(A.r64)[n] = make_double2(r0, r1);
+                            acc = fma(r0, r0, fma(r1, r1, acc));
+                        }
+                    }
+                    carry.x = y[0][2] + t3x;
+                    carry.y = y[1][2] + t3y;
+                }
+                plo = pj;
+                plr = pr;
+                if constexpr (MODE == MV_RESID) mprev = R.mj;
+            }
+        }
+        const bool last_of_prob = (w + 1 == kend);
+        if (last_of_prob || w + 1 == w1) {
+            double v[1] = {(double)acc}, tot[1];
+            if (warp_seg_flush<1>(v, A.partials, seg0, w + 1, kbeg, kend, &S.cnt[MODE == MV_PCG ? 0 : 1], tot) &&
+                lane == 0) {
+                if (MODE == MV_PCG) {
+                    S.pcg.pq = tot[0];
+                    if (!(tot[0] > 0.0) || !isfinite(tot[0])) {
+                        S.mode = M_RU;   // breakdown: refresh from the true residual
+                        request_refresh(A);
+                    } else {
+                        S.pcg.alpha = S.pcg.rz / tot[0];
                     }
                 } else {
-                    S.best = res;
+                    const double res = sqrt(tot[0]);
+                    S.res = res;
+                    if (!isfinite(res)) {
+                        S.mode = M_FAIL;
+                    } else if (res <= P.tol) {
+                        S.mode = (mode == M_RU) ? M_RU : M_DONE;   // M_RU: the rescale pass applies the last correction
+                        S.stall = -1;                                // converged marker for the rescale pass
+                    } else if (mode == M_RU) {
+                        if (res < 0.5 * S.best) {
+                            S.best = res;
+                            S.stall = 0;
+                        } else if (++S.stall >= 8) {
+                            S.mode = M_FAIL;
+                        }
+                    } else {
+                        S.best = res;
+                    }
                 }
             }
+            acc = Acc(0);
+            seg0 = w + 1;
+        }
+        if (last_of_prob && w + 1 < w1) {
+            ++k;
+            kbeg = kend;
+            kend = V.pref[k + 1];
         }
     }
 }
 
-// Reliable update / initialisation over node items (problems in M_INIT or M_RU):
-// u += s x32; then, unless converged, r32 = r64 / res, x32 = 0, the last
-// direction rescaled (M_RU) or cleared (M_INIT), and the PCG scalars rebuilt.
-// The last block of the grid sets the PCG-loop condition.
+// Reliable update / initialisation over the node chunks of listed problems in
+// M_INIT or M_RU: u += s x32; then, unless converged, r32 = r64 / res, x32 = 0,
+// the last direction rescaled (M_RU) or cleared (M_INIT), and the PCG scalars
+// rebuilt.  The last block of the grid rebuilds the active list and sets the
+// PCG-loop condition.
 __global__ void __launch_bounds__(kBThreads) bk_rescale(BArgs A) {
-    const Item it = A.nd[blockIdx.x];
-    const BProb P = A.P[it.prob];
-    BState& S = A.B[it.prob];
-    const int mode = S.mode;
-    const bool act = (mode == M_INIT || mode == M_RU);
-    const bool conv = act && S.stall == -1;
-    double v[2] = {0.0, 0.0};
-    if (act) {
+    __shared__ int s_pref[kListCache + 1], s_prob[kListCache];
+    const ListView V = load_list<false, kListCache>(A, kRefresh, s_pref, s_prob);
+    for (int w = blockIdx.x; w < V.total; w += gridDim.x) {
+        const int k = find_seg(V.pref, V.n, w);
+        const int p = V.prob[k];
+        BState& S = A.B[p];
+        const int mode = S.mode;
+        if (mode != M_INIT && mode != M_RU) {   // converged from the start (M_DONE) or failed
+            w = skip_to(w, V.pref[k + 1]);
+            continue;
+        }
+        const BProb& P = A.P[p];
+        const int c = w - V.pref[k];
+        const bool conv = S.stall == -1;
         const long long nnodes = (long long)P.nn[0] * P.nn[1];
         const double s_old = (mode == M_RU) ? S.s : 0.0;
         const double res = S.res;
@@ -498,14 +798,14 @@ __global__ void __launch_bounds__(kBThreads) bk_rescale(BArgs A) {
         float* plast = ((itn - 1) & 1) ? A.P1 : A.P0;
         const float ratio = (float)(res > 0.0 ? s_old / res : 0.0);
         float arz = 0.f, arr = 0.f;
-        for (int t = threadIdx.x; t < kNodeChunk; t += blockDim.x) {
-            const long long nl = (long long)it.a + t;
+        for (int tt = threadIdx.x; tt < kNodeChunk; tt += blockDim.x) {
+            const long long nl = (long long)c * kNodeChunk + tt;
             if (nl >= nnodes) break;
             const long long n = P.noff + nl;
             const float d = A.dinv32[n];
 #pragma unroll
-            for (int c = 0; c < 2; ++c) {
-                const long long i = 2 * n + c;
+            for (int cc = 0; cc < 2; ++cc) {
+                const long long i = 2 * n + cc;
                 if (mode == M_RU) A.u[i] = fma(s_old, (double)A.x32[i], A.u[i]);
                 if (!conv) {
                     const float rn = (float)(A.r64[i] * inv);
@@ -517,15 +817,13 @@ __global__ void __launch_bounds__(kBThreads) bk_rescale(BArgs A) {
                         A.P0[i] = 0.f;
                         A.P1[i] = 0.f;
                     }
-                    arz = fmaf(rn, d * A.Mf.kdinv[c] * rn, arz);
+                    arz = fmaf(rn, d * A.Mf.kdinv[cc] * rn, arz);
                     arr = fmaf(rn, rn, arr);
                 }
             }
         }
-        v[0] = arz;
-        v[1] = arr;
-        double tot[2];
-        if (prob_reduce_block<2>(v, A.partials, blockIdx.x, P.nd0, P.nnd, &S.cnt[2], tot)) {
+        double v[2] = {arz, arr}, tot[2];
+        if (prob_reduce_block<2>(v, A.partials, P.nd0 + c, P.nd0, P.nnd, &S.cnt[2], tot)) {
             if (threadIdx.x == 0) {
                 if (conv) {
                     S.mode = M_DONE;
@@ -535,6 +833,7 @@ __global__ void __launch_bounds__(kBThreads) bk_rescale(BArgs A) {
                         const double rz_prev = S.pcg.rz_old * q * q;
                         S.pcg.beta = rz_prev > 0.0 ? tot[0] / rz_prev : 0.0;
                         S.updates += 1;
+                        atomicAdd(&A.G->updates, 1);
                     } else {
                         S.pcg.beta = 0.0;
                         S.pcg.it = 0;
@@ -551,52 +850,73 @@ __global__ void __launch_bounds__(kBThreads) bk_rescale(BArgs A) {
                 }
             }
         }
+        __syncthreads();
     }
     if (grid_last(&A.G->cnt[0])) {
+        int failed = 0;
+        const int active = build_list(A, kActive, &failed);
         if (threadIdx.x == 0) {
-            int active = 0, failed = 0;
-            for (int b = 0; b < A.nprob; ++b) {
-                const int m = A.B[b].mode;
-                active += (m == M_PCG || m == M_RU);
-                failed += (m == M_FAIL);
-            }
-            A.G->loops += 1;
             A.G->active = active;
             A.G->failed = failed;
-            cudaGraphSetConditional(A.h_pcg, (active > 0 && A.G->loops < kMaxLoops) ? 1u : 0u);
+            if (A.in_graph) cudaGraphSetConditional(A.h_pcg, (active > 0 && A.G->loops < kMaxLoops) ? 1u : 0u);
+            if (A.in_loop) cudaGraphSetConditional(A.h_ru, 0u);
         }
     }
 }
 
-// PCG update over node items (M_PCG problems): x += alpha p, r -= alpha q, r.z, r.r
+// PCG update over the node chunks of listed problems in M_PCG:
+// x += alpha p, r -= alpha q, r.z, r.r
 __global__ void __launch_bounds__(kBThreads) bk_update(BArgs A) {
-    const Item it = A.nd[blockIdx.x];
-    const BProb P = A.P[it.prob];
-    BState& S = A.B[it.prob];
-    if (S.mode != M_PCG) return;
-    const int itn = S.pcg.it;
-    const float* __restrict__ p = (itn & 1) ? A.P1 : A.P0;
-    const float alpha = (float)S.pcg.alpha;
-    const long long nnodes = (long long)P.nn[0] * P.nn[1];
-    float arz = 0.f, arr = 0.f;
-    for (int t = threadIdx.x; t < kNodeChunk; t += blockDim.x) {
-        const long long nl = (long long)it.a + t;
-        if (nl >= nnodes) break;
-        const long long n = P.noff + nl;
-        const float d = A.dinv32[n];
-#pragma unroll
-        for (int c = 0; c < 2; ++c) {
-            const long long i = 2 * n + c;
-            A.x32[i] = fmaf(alpha, p[i], A.x32[i]);
-            const float rn = fmaf(-alpha, A.q32[i], A.r32[i]);
-            A.r32[i] = rn;
-            arz = fmaf(rn, d * A.Mf.kdinv[c] * rn, arz);
-            arr = fmaf(rn, rn, arr);
+    __shared__ int s_pref[kListCache + 1], s_prob[kListCache];
+    const ListView V = load_list<false, kListCache>(A, kActive, s_pref, s_prob);
+    int w, w1;
+    block_range(V.total, w, w1);
+    const float k0 = A.Mf.kdinv[0], k1 = A.Mf.kdinv[1];
+    const float2* __restrict__ qq = reinterpret_cast<const float2*>(A.q32);
+    float2* __restrict__ xx = reinterpret_cast<float2*>(A.x32);
+    float2* __restrict__ rr = reinterpret_cast<float2*>(A.r32);
+    while (w < w1) {
+        const int k = find_seg(V.pref, V.n, w);
+        const int kbeg = V.pref[k], kend = V.pref[k + 1];
+        const int wend = min(kend, w1);
+        const int p = V.prob[k];
+        BState& S = A.B[p];
+        if (S.mode != M_PCG) {   // broke down in the operator pass
+            w = wend;
+            continue;
         }
-    }
-    double v[2] = {arz, arr}, tot[2];
-    if (prob_reduce_block<2>(v, A.partials, blockIdx.x, P.nd0, P.nnd, &S.cnt[3], tot)) {
-        if (threadIdx.x == 0) {
+        const BProb& P = A.P[p];
+        const int itn = S.pcg.it;
+        const float2* __restrict__ pp = reinterpret_cast<const float2*>((itn & 1) ? A.P1 : A.P0);
+        const float alpha = (float)S.pcg.alpha;
+        const long long nnodes = (long long)P.nn[0] * P.nn[1];
+        const long long nb = (long long)(w - kbeg) * kNodeChunk;
+        const long long ne = min(nnodes, (long long)(wend - kbeg) * kNodeChunk);
+        float arz = 0.f, arr = 0.f;
+        for (long long base = nb; base < ne; base += 4 * kBThreads) {
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const long long nl = base + u * kBThreads + threadIdx.x;
+                if (nl < ne) {
+                    const long long n = P.noff + nl;
+                    const float d = A.dinv32[n];
+                    const float2 pv = pp[n], qv = qq[n];
+                    float2 xv = xx[n], rv = rr[n];
+                    xv.x = fmaf(alpha, pv.x, xv.x);
+                    xv.y = fmaf(alpha, pv.y, xv.y);
+                    rv.x = fmaf(-alpha, qv.x, rv.x);
+                    rv.y = fmaf(-alpha, qv.y, rv.y);
+                    xx[n] = xv;
+                    rr[n] = rv;
+                    arz = fmaf(rv.x, d * k0 * rv.x, arz);
+                    arz = fmaf(rv.y, d * k1 * rv.y, arz);
+                    arr = fmaf(rv.x, rv.x, arr);
+                    arr = fmaf(rv.y, rv.y, arr);
+                }
+            }
+        }
+        double v[2] = {arz, arr}, tot[2];
+        if (seg_flush<2>(v, A.partials, w, wend, kbeg, kend, &S.cnt[3], tot) && threadIdx.x == 0) {
             PcgState& st = S.pcg;
             const double rzo = st.rz;
             st.rz_old = rzo;
@@ -604,14 +924,21 @@ __global__ void __launch_bounds__(kBThreads) bk_update(BArgs A) {
             st.beta = rzo != 0.0 ? tot[0] / rzo : 0.0;
             st.rr = tot[1];
             st.it = itn + 1;
-            if (!isfinite(tot[1]) || tot[1] <= st.tol2 || tot[1] < st.ru_delta2 * st.rr_max)
+            if (!isfinite(tot[1]) || tot[1] <= st.tol2 || tot[1] < st.ru_delta2 * st.rr_max ||
+                itn + 1 >= st.maxit) {   // at maxit the refresh pass decides (and fails the problem)
                 S.mode = M_RU;
-            else if (itn + 1 >= st.maxit)
-                S.mode = M_RU;   // the update pass decides (fails when maxit is spent)
+                request_refresh(A);
+            }
             st.rr_max = fmax(st.rr_max, tot[1]);
         }
+        __syncthreads();
+        w = wend;
     }
 }
+
+
+// refresh list of the problems that asked for the FP64 residual in this loop
+__global__ void bk_rulist(BArgs A) { build_list(A, kRefresh, nullptr); }
 
 // ---- compliance + sensitivities (FP64, cell items) ----
 __global__ void __launch_bounds__(kBThreads) bk_compliance(BArgs A) {
@@ -697,11 +1024,16 @@ __global__ void __launch_bounds__(kBThreads) bk_oc_step(BArgs A) {
         }
     }
     if (grid_last(&A.G->cnt[1])) {
+        __shared__ int s_act;
+        if (threadIdx.x == 0) s_act = 0;
+        __syncthreads();
+        int act = 0;
+        for (int b = threadIdx.x; b < A.nprob; b += blockDim.x) act += !*(volatile const int*)&A.B[b].oc.done;
+        if (act) atomicAdd(&s_act, act);
+        __syncthreads();
         if (threadIdx.x == 0) {
-            int act = 0;
-            for (int b = 0; b < A.nprob; ++b) act += !A.B[b].oc.done;
-            A.G->oc_active = act;
-            cudaGraphSetConditional(A.h_oc, act > 0 ? 1u : 0u);
+            A.G->oc_active = s_act;
+            if (A.in_graph) cudaGraphSetConditional(A.h_oc, s_act > 0 ? 1u : 0u);
         }
     }
 }
@@ -742,9 +1074,11 @@ __global__ void __launch_bounds__(kBThreads) bk_copy(double* __restrict__ dst, c
 struct tog_batch {
     int nprob = 0;
     std::vector<BProb> probs;
-    std::vector<Item> mv, nd, ce;
+    std::vector<Item> nd, ce;
     long long nnodes = 0, ncells = 0;
-    int LY = 32;
+    int LY = 32;                 // node rows per operator item (autotuned)
+    int gt = 0, gr = 0, gn = 0;  // persistent grids: FP32 operator, FP64 residual, node passes
+    int grid_div = 1;            // FP32 operator grid = occupancy limit / grid_div (autotuned)
     double xmin = 1e-9, pen = 3.0, rtol = 1e-8, move = 0.2;
     int maxit = 1 << 20;
     cudaStream_t own = nullptr, stream = nullptr;
@@ -753,14 +1087,14 @@ struct tog_batch {
     BProb* d_P = nullptr;
     BState* d_B = nullptr;
     BGlobal* d_G = nullptr;
-    Item *d_mv = nullptr, *d_nd = nullptr, *d_ce = nullptr;
+    Item *d_nd = nullptr, *d_ce = nullptr;
     std::vector<void*> allocs;
     BArgs A{};
     std::vector<BState> h_B;
     BGlobal* h_G = nullptr;
     cudaGraphExec_t exec = nullptr;
     cudaGraph_t graph = nullptr;
-    cudaGraphConditionalHandle h_pcg{}, h_oc{};
+    cudaGraphConditionalHandle h_pcg{}, h_oc{}, h_ru{};
     int steps = 0;
 };
 
@@ -784,17 +1118,50 @@ int balloc(tog_batch* b, T** p, size_t n) {
     return TOG_OK;
 }
 
-void build_mv_items(tog_batch* b, int LY) {
-    b->mv.clear();
+// march items per problem: strips of 30 owned node columns x bands of LY node
+// rows; returns the total
+long long build_tiles(tog_batch* b, int LY) {
+    long long t = 0;
     for (int p = 0; p < b->nprob; ++p) {
         BProb& P = b->probs[p];
-        P.mv0 = (int)b->mv.size();
-        const int tx = (P.nn[0] + 30) / 31;
-        const int ty = (P.nn[1] + LY - 1) / LY;
-        for (int y = 0; y < ty; ++y)
-            for (int x = 0; x < tx; ++x) b->mv.push_back(Item{p, x, y * LY});
-        P.nmv = (int)b->mv.size() - P.mv0;
+        P.ntx = (P.nn[0] + 29) / 30;
+        P.t0 = (int)t;
+        P.nt = P.ntx * ((P.nn[1] + LY - 1) / LY);
+        t += P.nt;
     }
+    return t;
+}
+
+int blocks_per_sm(const void* fn, int threads, size_t smem = 0) {
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, threads, smem) != cudaSuccess || nb < 1) nb = 1;
+    return nb;
+}
+
+void launch_mvpcg(const BArgs& A, int grid, cudaStream_t s) {
+    bk_march<float, MV_PCG><<<grid, 32 * kMarchWarps, 0, s>>>(A);
+}
+void launch_resid(const BArgs& A, int grid, cudaStream_t s) {
+    bk_march<double, MV_RESID><<<grid, 32 * kMarchWarps, 0, s>>>(A);
+}
+
+// persistent grid sizes; frac_div divides the FP32 operator's grid
+void set_grids(tog_batch* b, int frac_div) {
+    b->gt = std::max(1, b->nsm * blocks_per_sm((const void*)bk_march<float, MV_PCG>, 32 * kMarchWarps) / frac_div);
+    b->gr = b->nsm * blocks_per_sm((const void*)bk_march<double, MV_RESID>, 32 * kMarchWarps);
+    b->gn = b->nsm * blocks_per_sm((const void*)bk_update, kBThreads);
+}
+
+// design-iteration set-up: filter, element scales, Jacobi diagonal, FP64
+// residual of the warm start, PCG initialisation (and the first active list)
+void launch_setup(tog_batch* b, const BArgs& A, cudaStream_t s) {
+    bk_begin<<<1, 256, 0, s>>>(A);
+    bk_filt_nodeavg<<<A.nnd, kBThreads, 0, s>>>(A, A.x, A.nodal);
+    bk_filt_cone<<<A.nce, kBThreads, 0, s>>>(A, A.nodal, A.x, A.vars);
+    bk_escale<<<A.nce, kBThreads, 0, s>>>(A);
+    bk_nodesum<<<A.nnd, kBThreads, 0, s>>>(A);
+    launch_resid(A, b->gr, s);
+    bk_rescale<<<b->gn, kBThreads, 0, s>>>(A);
 }
 
 // record the whole design iteration into b->graph (kernels + two conditional WHILE nodes)
@@ -812,9 +1179,11 @@ int build_graph(tog_batch* b) {
     TB_CUDA(cudaGraphConditionalHandleCreate(&b->h_oc, b->graph, 1, cudaGraphCondAssignDefault));
     b->A.h_pcg = b->h_pcg;
     b->A.h_oc = b->h_oc;
+    b->A.in_graph = 1;
+    b->A.in_loop = 0;
+    b->A.LY = b->LY;
     const BArgs A = b->A;
     cudaStream_t s = b->own;
-    const int nmvb = (b->A.nmv + kMvWarps - 1) / kMvWarps;
     const int nce = b->A.nce, nnd = b->A.nnd;
     auto tail = [&](std::vector<cudaGraphNode_t>& deps) -> int {
         cudaStreamCaptureStatus st;
@@ -827,13 +1196,7 @@ int build_graph(tog_batch* b) {
     std::vector<cudaGraphNode_t> deps;
     // segment 1: filter, scales, initial FP64 residual and PCG set-up
     TB_CUDA(cudaStreamBeginCaptureToGraph(s, b->graph, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-    bk_begin<<<1, 256, 0, s>>>(A);
-    bk_filt_nodeavg<<<nnd, kBThreads, 0, s>>>(A, A.x, A.nodal);
-    bk_filt_cone<<<nce, kBThreads, 0, s>>>(A, A.nodal, A.x, A.vars);
-    bk_escale<<<nce, kBThreads, 0, s>>>(A);
-    bk_nodesum<<<nnd, kBThreads, 0, s>>>(A);
-    bk_matvec<double, MV_RESID><<<nmvb, 32 * kMvWarps, 0, s>>>(A);
-    bk_rescale<<<nnd, kBThreads, 0, s>>>(A);
+    launch_setup(b, A, s);
     {
         int rc = tail(deps);
         if (rc != TOG_OK) return rc;
@@ -848,14 +1211,36 @@ int build_graph(tog_batch* b) {
     cp.conditional.size = 1;
     cudaGraphNode_t wpcg;
     TB_CUDA(cudaGraphAddNode(&wpcg, b->graph, deps.data(), nullptr, deps.size(), &cp));
+    // body: FP32 operator + update every loop; the FP64 refresh pass (refresh list,
+    // true residual, rescale) only in loops where some problem asked for it
     cudaGraph_t body = cp.conditional.phGraph_out[0];
+    TB_CUDA(cudaGraphConditionalHandleCreate(&b->h_ru, body, 0, cudaGraphCondAssignDefault));
+    BArgs AL = A;
+    AL.in_loop = 1;
+    AL.h_ru = b->h_ru;
     TB_CUDA(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-    bk_matvec<float, MV_PCG><<<nmvb, 32 * kMvWarps, 0, s>>>(A);
-    bk_update<<<nnd, kBThreads, 0, s>>>(A);
-    bk_matvec<double, MV_RESID><<<nmvb, 32 * kMvWarps, 0, s>>>(A);
-    bk_rescale<<<nnd, kBThreads, 0, s>>>(A);
+    launch_mvpcg(AL, b->gt, s);
+    bk_update<<<b->gn, kBThreads, 0, s>>>(AL);
+    {
+        int rc = tail(deps);
+        if (rc != TOG_OK) return rc;
+    }
     cudaGraph_t gb;
     TB_CUDA(cudaStreamEndCapture(s, &gb));
+    cudaGraphNodeParams ci{};
+    ci.type = cudaGraphNodeTypeConditional;
+    ci.conditional.handle = b->h_ru;
+    ci.conditional.type = cudaGraphCondTypeIf;
+    ci.conditional.size = 1;
+    cudaGraphNode_t nif;
+    TB_CUDA(cudaGraphAddNode(&nif, body, deps.data(), nullptr, deps.size(), &ci));
+    cudaGraph_t ibody = ci.conditional.phGraph_out[0];
+    TB_CUDA(cudaStreamBeginCaptureToGraph(s, ibody, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    bk_rulist<<<1, 256, 0, s>>>(AL);
+    launch_resid(AL, b->gr, s);
+    bk_rescale<<<b->gn, kBThreads, 0, s>>>(AL);
+    cudaGraph_t gib;
+    TB_CUDA(cudaStreamEndCapture(s, &gib));
     // segment 2: compliance, filter pullback, OC prep
     cudaGraphNode_t d1[1] = {wpcg};
     TB_CUDA(cudaStreamBeginCaptureToGraph(s, b->graph, d1, nullptr, 1, cudaStreamCaptureModeThreadLocal));
@@ -928,6 +1313,17 @@ int tog_batch_create(int32_t nprob, const int32_t* nelx, const int32_t* nely, co
         Md.kdinv[c] = 1.0 / kd[c];
         Mf.kdinv[c] = (float)(1.0 / kd[c]);
     }
+    // corner-ordered element block for the FP32 gather: corner n = bx + 2 by holds
+    // Ferrite node a with kFerriteToCorner[a] = n, whose dofs are 2 a + c in Ke
+    float Kc[2][4][2][4];
+    {
+        int c2f[4];
+        for (int a = 0; a < 4; ++a) c2f[kFerriteToCorner[a]] = a;
+        for (int c = 0; c < 2; ++c)
+            for (int i = 0; i < 4; ++i)
+                for (int d = 0; d < 2; ++d)
+                    for (int j = 0; j < 4; ++j) Kc[c][i][d][j] = (float)Ke[(2 * c2f[i] + c) * 8 + 2 * c2f[j] + d];
+    }
     // problems, items, stencils, boundary conditions and loads
     std::vector<int> soff;
     std::vector<double> sw;
@@ -970,7 +1366,12 @@ int tog_batch_create(int32_t nprob, const int32_t* nelx, const int32_t* nely, co
     }
     b->nnodes = noff;
     b->ncells = eoff;
-    build_mv_items(b, b->LY);
+    const long long max_tiles = build_tiles(b, 8);   // the lowest band gives the most items
+    build_tiles(b, b->LY);
+    if (max_tiles > (1LL << 30)) {
+        delete b;
+        return bfail(TOG_ERR_ARG, "tog_batch_create: batch too large");
+    }
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&b->nsm, cudaDevAttrMultiProcessorCount, dev);
@@ -992,7 +1393,11 @@ int tog_batch_create(int32_t nprob, const int32_t* nelx, const int32_t* nely, co
     R(balloc(b, &b->d_P, nprob));
     R(balloc(b, &b->d_B, nprob));
     R(balloc(b, &b->d_G, 1));
-    R(balloc(b, &b->d_mv, b->mv.size() + 4 * 64));
+    for (int l = 0; l < 2; ++l) {
+        R(balloc(b, &A.lst[l].prob, nprob + 1));
+        R(balloc(b, &A.lst[l].tpref, nprob + 1));
+        R(balloc(b, &A.lst[l].npref, nprob + 1));
+    }
     R(balloc(b, &b->d_nd, b->nd.size()));
     R(balloc(b, &b->d_ce, b->ce.size()));
     R(balloc(b, &fixmask, NN));
@@ -1018,7 +1423,7 @@ int tog_batch_create(int32_t nprob, const int32_t* nelx, const int32_t* nely, co
     R(balloc(b, &A.invW, NC));
     R(balloc(b, &d_soff, soff.size()));
     R(balloc(b, &d_sw, sw.size()));
-    const size_t nitems = std::max(b->mv.size() + 4 * 64, std::max(b->nd.size(), b->ce.size()));
+    const size_t nitems = std::max((size_t)max_tiles, std::max(b->nd.size(), b->ce.size()));
     R(balloc(b, &A.partials, 2 * nitems + 64));
     if (rc != TOG_OK) {
         std::string m = tog_last_error();
@@ -1037,14 +1442,13 @@ int tog_batch_create(int32_t nprob, const int32_t* nelx, const int32_t* nely, co
     A.P = b->d_P;
     A.B = b->d_B;
     A.G = b->d_G;
-    A.mv = b->d_mv;
     A.nd = b->d_nd;
     A.ce = b->d_ce;
-    A.nmv = (int)b->mv.size();
     A.nnd = (int)b->nd.size();
     A.nce = (int)b->ce.size();
     A.nprob = nprob;
     A.LY = b->LY;
+    std::memcpy(A.Kc, Kc, sizeof(Kc));
     A.fixmask = fixmask;
     A.f = f;
     A.soff = d_soff;
@@ -1063,7 +1467,6 @@ int tog_batch_create(int32_t nprob, const int32_t* nelx, const int32_t* nely, co
         if (e == cudaSuccess) e = x;
     };
     C(cudaMemcpyAsync(b->d_P, b->probs.data(), nprob * sizeof(BProb), cudaMemcpyHostToDevice, b->own));
-    C(cudaMemcpyAsync(b->d_mv, b->mv.data(), b->mv.size() * sizeof(Item), cudaMemcpyHostToDevice, b->own));
     C(cudaMemcpyAsync(b->d_nd, b->nd.data(), b->nd.size() * sizeof(Item), cudaMemcpyHostToDevice, b->own));
     C(cudaMemcpyAsync(b->d_ce, b->ce.data(), b->ce.size() * sizeof(Item), cudaMemcpyHostToDevice, b->own));
     C(cudaMemcpyAsync(fixmask, hm.data(), NN, cudaMemcpyHostToDevice, b->own));
@@ -1106,6 +1509,7 @@ int tog_batch_create(int32_t nprob, const int32_t* nelx, const int32_t* nely, co
         return bfail(TOG_ERR_CUDA, std::string("batch init: ") + cudaGetErrorString(e));
     }
     b->h_B.resize(nprob);
+    set_grids(b, b->grid_div);
     rc = build_graph(b);
     if (rc != TOG_OK) {
         std::string m = tog_last_error();
@@ -1147,6 +1551,7 @@ int tog_batch_step(tog_batch* b, tog_batch_stats* stats) {
         stats->pcg_loops = b->h_G->loops;
         stats->failed = b->h_G->failed;
         stats->steps = b->steps;
+        stats->reliable_updates = b->h_G->updates;
     }
     if (b->h_G->failed > 0)
         return bfail(TOG_NOT_CONVERGED, std::to_string(b->h_G->failed) + " problem(s) of the batch did not converge");
@@ -1165,6 +1570,19 @@ int tog_batch_results(tog_batch* b, double* compliance, double* change, int32_t*
     return TOG_OK;
 }
 
+int tog_batch_solve_info(tog_batch* b, double* residual, int32_t* refreshes, int32_t* status) {
+    if (!b) return bfail(TOG_ERR_ARG, "null batch");
+    TB_CUDA(cudaMemcpyAsync(b->h_B.data(), b->d_B, b->nprob * sizeof(BState), cudaMemcpyDeviceToHost, b->stream));
+    TB_CUDA(cudaStreamSynchronize(b->stream));
+    for (int p = 0; p < b->nprob; ++p) {
+        const BState& S = b->h_B[p];
+        if (residual) residual[p] = S.res;
+        if (refreshes) refreshes[p] = S.updates;
+        if (status) status[p] = S.mode == M_DONE ? TOG_OK : S.mode == M_FAIL ? TOG_NOT_CONVERGED : TOG_ERR_STATE;
+    }
+    return TOG_OK;
+}
+
 int tog_batch_get_design(tog_batch* b, int32_t prob, double* x) {
     if (!b || !x || prob < 0 || prob >= b->nprob) return bfail(TOG_ERR_ARG, "bad batch design request");
     const BProb& P = b->probs[prob];
@@ -1174,69 +1592,136 @@ int tog_batch_get_design(tog_batch* b, int32_t prob, double* x) {
     return TOG_OK;
 }
 
-int tog_batch_autotune(tog_batch* b, int32_t* ly_out) {
+int tog_batch_set_tile_rows(tog_batch* b, int32_t tile_rows) {
+    if (!b || (tile_rows != 8 && tile_rows != 16 && tile_rows != 32 && tile_rows != 64))
+        return bfail(TOG_ERR_ARG, "tog_batch_set_tile_rows: rows must be 8, 16, 32 or 64");
+    TB_CUDA(cudaStreamSynchronize(b->stream));
+    b->LY = tile_rows;
+    b->grid_div = 1;
+    build_tiles(b, tile_rows);
+    TB_CUDA(cudaMemcpy(b->d_P, b->probs.data(), b->nprob * sizeof(BProb), cudaMemcpyHostToDevice));
+    set_grids(b, 1);
+    b->A.LY = tile_rows;
+    return build_graph(b);
+}
+
+int tog_batch_autotune(tog_batch* b, int32_t* tile_rows) {
     if (!b) return bfail(TOG_ERR_ARG, "null batch");
-    // time the FP32 operator over all problems for each candidate chunk height and keep the fastest
-    const int cand[] = {8, 16, 32, 64, 128};
+    TB_CUDA(cudaStreamSynchronize(b->stream));
+    // Every candidate (tile rows x grid size of the FP32 operator) is timed on
+    // PCG iterations of all problems at once.  The PCG state comes from the
+    // set-up kernels of a design iteration run outside the graph, with reliable
+    // updates switched off so that every problem keeps iterating; only scratch
+    // vectors change (the next design iteration rebuilds them).
+    cudaStream_t s = b->own;
+    const int cand_ty[] = {8, 16, 32, 64};
+    const int cand_div[] = {1, 2, 4};
     float best_ms = 1e30f;
-    int best = b->LY;
+    int best_ty = b->LY, best_div = b->grid_div;
     cudaEvent_t e0, e1;
     TB_CUDA(cudaEventCreate(&e0));
     TB_CUDA(cudaEventCreate(&e1));
-    // operator inputs: every problem in PCG mode with beta = 0 (state only read by the operator)
-    std::vector<BState> hb(b->nprob);
-    TB_CUDA(cudaMemcpy(hb.data(), b->d_B, b->nprob * sizeof(BState), cudaMemcpyDeviceToHost));
-    std::vector<BState> tb = hb;
-    for (auto& s : tb) {
-        s.mode = M_PCG;
-        s.pcg.beta = 0.0;
-    }
-    for (int ly : cand) {
-        build_mv_items(b, ly);
-        TB_CUDA(cudaFree(b->d_mv));
-        b->allocs.erase(std::remove(b->allocs.begin(), b->allocs.end(), (void*)b->d_mv), b->allocs.end());
-        int rc = balloc(b, &b->d_mv, b->mv.size() + 4 * 64);
-        if (rc != TOG_OK) return rc;
-        TB_CUDA(cudaMemcpy(b->d_mv, b->mv.data(), b->mv.size() * sizeof(Item), cudaMemcpyHostToDevice));
-        TB_CUDA(cudaMemcpy(b->d_P, b->probs.data(), b->nprob * sizeof(BProb), cudaMemcpyHostToDevice));
+    int rc = TOG_OK;
+    for (int ty : cand_ty) {
+        build_tiles(b, ty);
+        TB_CUDA(cudaMemcpyAsync(b->d_P, b->probs.data(), b->nprob * sizeof(BProb), cudaMemcpyHostToDevice, s));
+        b->LY = ty;
+        set_grids(b, 1);
         BArgs A = b->A;
-        A.mv = b->d_mv;
-        A.nmv = (int)b->mv.size();
-        A.LY = ly;
-        const int nmvb = (A.nmv + kMvWarps - 1) / kMvWarps;
-        for (int rep = 0; rep < 2; ++rep) {
-            TB_CUDA(cudaMemcpy(b->d_B, tb.data(), b->nprob * sizeof(BState), cudaMemcpyHostToDevice));
-            bk_matvec<float, MV_PCG><<<nmvb, 32 * kMvWarps, 0, b->own>>>(A);
-        }
-        TB_CUDA(cudaEventRecord(e0, b->own));
-        for (int rep = 0; rep < 10; ++rep) bk_matvec<float, MV_PCG><<<nmvb, 32 * kMvWarps, 0, b->own>>>(A);
-        TB_CUDA(cudaEventRecord(e1, b->own));
-        TB_CUDA(cudaEventSynchronize(e1));
-        float ms = 0.f;
-        TB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-        if (ms < best_ms) {
-            best_ms = ms;
-            best = ly;
+        A.in_graph = 0;
+        A.ru_delta2 = 0.0;
+        A.LY = ty;
+        launch_setup(b, A, s);
+        for (int div : cand_div) {
+            set_grids(b, div);
+            for (int rep = 0; rep < 3; ++rep) {
+                launch_mvpcg(A, b->gt, s);
+                bk_update<<<b->gn, kBThreads, 0, s>>>(A);
+            }
+            TB_CUDA(cudaEventRecord(e0, s));
+            for (int rep = 0; rep < 10; ++rep) {
+                launch_mvpcg(A, b->gt, s);
+                bk_update<<<b->gn, kBThreads, 0, s>>>(A);
+            }
+            TB_CUDA(cudaEventRecord(e1, s));
+            TB_CUDA(cudaEventSynchronize(e1));
+            TB_CUDA(cudaGetLastError());
+            float ms = 0.f;
+            TB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            if (ms < best_ms) {
+                best_ms = ms;
+                best_ty = ty;
+                best_div = div;
+            }
         }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    TB_CUDA(cudaMemcpy(b->d_B, hb.data(), b->nprob * sizeof(BState), cudaMemcpyHostToDevice));
-    // rebuild items with the winner and re-record the graph
-    build_mv_items(b, best);
-    TB_CUDA(cudaFree(b->d_mv));
-    b->allocs.erase(std::remove(b->allocs.begin(), b->allocs.end(), (void*)b->d_mv), b->allocs.end());
-    int rc = balloc(b, &b->d_mv, b->mv.size() + 4 * 64);
-    if (rc != TOG_OK) return rc;
-    TB_CUDA(cudaMemcpy(b->d_mv, b->mv.data(), b->mv.size() * sizeof(Item), cudaMemcpyHostToDevice));
-    TB_CUDA(cudaMemcpy(b->d_P, b->probs.data(), b->nprob * sizeof(BProb), cudaMemcpyHostToDevice));
-    b->LY = best;
-    b->A.mv = b->d_mv;
-    b->A.nmv = (int)b->mv.size();
-    b->A.LY = best;
+    b->LY = best_ty;
+    b->grid_div = best_div;
+    build_tiles(b, best_ty);
+    TB_CUDA(cudaMemcpyAsync(b->d_P, b->probs.data(), b->nprob * sizeof(BProb), cudaMemcpyHostToDevice, s));
+    TB_CUDA(cudaStreamSynchronize(s));
+    set_grids(b, best_div);
+    b->A.LY = best_ty;
     rc = build_graph(b);
     if (rc != TOG_OK) return rc;
-    if (ly_out) *ly_out = best;
+    if (tile_rows) *tile_rows = best_ty;
+    return TOG_OK;
+}
+
+// Measurement hooks.  Launch one loop kernel nlaunch times over ALL problems of
+// the batch on the batch's stream and return the mean time per launch (CUDA
+// events).  State: the set-up kernels of a design iteration run first, outside
+// the graph (reliable updates off, so every problem stays in PCG mode); only
+// solver scratch changes, the design and displacements do not.
+//   kernel 0: FP32 operator (p update, K p, p.q)    1: PCG vector update
+//   kernel 2: FP64 true residual                      3: operator + update (one loop)
+int tog_batch_bench_kernel(tog_batch* b, int32_t kernel, int32_t nlaunch, double* us_per_launch) {
+    if (!b || kernel < 0 || kernel > 3 || nlaunch < 1 || !us_per_launch)
+        return bfail(TOG_ERR_ARG, "tog_batch_bench_kernel: bad arguments");
+    TB_CUDA(cudaStreamSynchronize(b->stream));
+    cudaStream_t s = b->own;
+    BArgs A = b->A;
+    A.in_graph = 0;
+    A.in_loop = 0;
+    A.ru_delta2 = 0.0;
+    launch_setup(b, A, s);
+    if (kernel == 2) bk_begin<<<1, 256, 0, s>>>(A);   // every problem listed for the residual, mode M_INIT
+    auto one = [&]() {
+        if (kernel == 0 || kernel == 3) launch_mvpcg(A, b->gt, s);
+        if (kernel == 1 || kernel == 3) bk_update<<<b->gn, kBThreads, 0, s>>>(A);
+        if (kernel == 2) launch_resid(A, b->gr, s);
+    };
+    for (int i = 0; i < 3; ++i) one();
+    cudaEvent_t e0, e1;
+    TB_CUDA(cudaEventCreate(&e0));
+    TB_CUDA(cudaEventCreate(&e1));
+    TB_CUDA(cudaEventRecord(e0, s));
+    for (int i = 0; i < nlaunch; ++i) one();
+    TB_CUDA(cudaEventRecord(e1, s));
+    TB_CUDA(cudaEventSynchronize(e1));
+    TB_CUDA(cudaGetLastError());
+    float ms = 0.f;
+    TB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *us_per_launch = 1e3 * (double)ms / nlaunch;
+    return TOG_OK;
+}
+
+// Algorithmic HBM bytes of one launch of those kernels over all problems: each
+// array element read or written once (halo re-reads and scalars excluded).
+int tog_batch_kernel_bytes(tog_batch* b, int32_t kernel, double* bytes) {
+    if (!b || kernel < 0 || kernel > 3 || !bytes) return bfail(TOG_ERR_ARG, "tog_batch_kernel_bytes: bad arguments");
+    const double N = (double)b->nnodes, C = (double)b->ncells;
+    // operator: r32, p_old (8+8), dinv (4), fixed mask (1) in; p, q (8+8) out; densities (4 per cell)
+    const double op = 37.0 * N + 4.0 * C;
+    // update: p, q, x, r (4 x 8), dinv (4) in; x, r (2 x 8) out
+    const double up = 52.0 * N;
+    // residual: u (16), x32 (8), mask (1), f (16) in; r64 (16) out; densities (8 per cell)
+    const double rs = 57.0 * N + 8.0 * C;
+    *bytes = kernel == 0 ? op : kernel == 1 ? up : kernel == 2 ? rs : op + up;
     return TOG_OK;
 }
 

@@ -421,6 +421,10 @@ class BatchedSIMP:
         L.check(L.lib().tog_batch_autotune(self.handle, L.C.byref(ly)))
         return ly.value
 
+    def set_tile_rows(self, rows):
+        """Pin the operator's band height (8, 16, 32 or 64 node rows per work item)."""
+        L.check(L.lib().tog_batch_set_tile_rows(self.handle, int(rows)))
+
     def set_stream(self, stream_ptr):
         L.check(L.lib().tog_batch_set_stream(self.handle, L.C.c_void_p(stream_ptr)))
 
@@ -436,7 +440,24 @@ class BatchedSIMP:
         L.check(L.lib().tog_batch_results(self.handle, L.dptr(c), L.dptr(ch), L.iptr(it)))
         return c, ch, it
 
+    def solve_info(self):
+        """Per problem: final FP64 residual norm, reliable updates, status code."""
+        res = np.empty(self.nprob)
+        ref = np.empty(self.nprob, dtype=np.int32)
+        stt = np.empty(self.nprob, dtype=np.int32)
+        L.check(L.lib().tog_batch_solve_info(self.handle, L.dptr(res), L.iptr(ref), L.iptr(stt)))
+        return res, ref, stt
+
     def design(self, p):
         x = np.empty(int(self.nelx[p]) * int(self.nely[p]))
         L.check(L.lib().tog_batch_get_design(self.handle, int(p), L.dptr(x)))
         return x
+
+    def bench_kernel(self, kernel, nlaunch=20):
+        """Mean microseconds per launch of one PCG-loop kernel over all problems
+        (0 operator, 1 update, 2 FP64 residual, 3 operator + update) and its
+        algorithmic bytes.  Changes only solver scratch."""
+        us, by = L.C.c_double(), L.C.c_double()
+        L.check(L.lib().tog_batch_bench_kernel(self.handle, int(kernel), int(nlaunch), L.C.byref(us)))
+        L.check(L.lib().tog_batch_kernel_bytes(self.handle, int(kernel), L.C.byref(by)))
+        return us.value, by.value
