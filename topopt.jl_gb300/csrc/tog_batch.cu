@@ -87,7 +87,6 @@ struct BArgs {
     int in_graph;               // kernels set graph conditions only inside the graph
     int in_loop;                // ... and the refresh condition only inside the PCG loop body
     WList lst[2];
-    const uint8_t* fixmask;
     const double* f;
     double *u, *r64;
     float *x32, *r32, *P0, *P1, *q32, *dinv32, *e32;
@@ -590,33 +589,40 @@ __device__ bool warp_seg_flush(double (&v)[NV], double* partials, int seg0, int 
     return true;
 }
 
+#ifndef TOG_MARCH_DEPTH
+#define TOG_MARCH_DEPTH 7
+#endif
+constexpr int kMarchDepth = TOG_MARCH_DEPTH;   // rows the FP32 operator loads ahead
+
 template <typename T, int MODE>
 struct MarchRow;
 template <>
-struct MarchRow<float, MV_PCG> {   // raw inputs of node row j (and element / mask of row j - 1)
+struct MarchRow<float, MV_PCG> {   // raw inputs of node row j and the density of element row j - 1
     float2 r, po;
     float d, rho;
-    unsigned m;
 };
 template <>
-struct MarchRow<double, MV_RESID> {
+struct MarchRow<double, MV_RESID> {   // ... and the load of node row j - 1
     double2 u, f;
     float2 xs;
     double rho;
-    unsigned mj;   // fixed mask of row j (zeroes v)
 };
 
 constexpr int kMarchWarps = 8;   // warps per block
+constexpr int kMarchList = 1024; // work-list entries a block keeps in shared memory
+
+// The batch's problems are clamped along the left edge (x = 0) and nowhere else,
+// so the fixed-dof mask of a node is a function of its column.
 
 template <typename T, int MODE>
 __global__ void __launch_bounds__(32 * kMarchWarps) bk_march(BArgs A) {
-    constexpr int D = (MODE == MV_PCG) ? 4 : 2;   // rows loaded ahead
+    constexpr int D = (MODE == MV_PCG) ? kMarchDepth : 2;   // rows loaded ahead (register ring)
     using Row = MarchRow<T, MODE>;
     using Acc = typename std::conditional<MODE == MV_PCG, float, double>::type;
     using V2 = typename std::conditional<MODE == MV_PCG, float2, double2>::type;
-    __shared__ int s_pref[kListCache + 1], s_prob[kListCache];
+    __shared__ int s_pref[kMarchList + 1], s_prob[kMarchList];
     if (MODE == MV_PCG && blockIdx.x == 0 && threadIdx.x == 0) A.G->loops += 1;
-    const ListView V = load_list<true, kListCache>(A, MODE == MV_PCG ? kActive : kRefresh, s_pref, s_prob);
+    const ListView V = load_list<true, kMarchList>(A, MODE == MV_PCG ? kActive : kRefresh, s_pref, s_prob);
     const int lane = threadIdx.x & 31;
     const int GW = gridDim.x * kMarchWarps;
     const int gw = blockIdx.x * kMarchWarps + (threadIdx.x >> 5);
@@ -640,6 +646,7 @@ __global__ void __launch_bounds__(32 * kMarchWarps) bk_march(BArgs A) {
         const bool colok = x >= 0 && x < nnx;
         const bool elok = x >= 0 && x < nelx && lane < 31;
         const bool own = colok && lane >= 1 && lane <= 30;
+        const bool fixed = (x == 0);
         const long long nb = P.noff + x, eb = P.eoff + x;
         // per-item scalars and row loader
         T beta = T(0), sc = T(0);
@@ -662,11 +669,9 @@ __global__ void __launch_bounds__(32 * kMarchWarps) bk_march(BArgs A) {
                 R.po = rok ? pold[n] : make_float2(0.f, 0.f);
                 R.d = rok ? A.dinv32[n] : 0.f;
                 R.rho = eok ? A.e32[e] : 0.f;
-                R.m = (own && j >= 1) ? (unsigned)A.fixmask[n - nnx] : 0u;
             } else {
                 R.u = rok ? reinterpret_cast<const double2*>(A.u)[n] : make_double2(0.0, 0.0);
                 R.xs = rok ? reinterpret_cast<const float2*>(A.x32)[n] : make_float2(0.f, 0.f);
-                R.mj = rok ? (unsigned)A.fixmask[n] : 0u;
                 R.rho = eok ? A.e64[e] : 0.0;
                 R.f = (own && j >= 1) ? reinterpret_cast<const double2*>(A.f)[n - nnx] : make_double2(0.0, 0.0);
             }
@@ -677,7 +682,6 @@ __global__ void __launch_bounds__(32 * kMarchWarps) bk_march(BArgs A) {
         for (int s = 0; s < D; ++s)
             if (j0 + s <= j1) load(j0 + s, buf[s]);
         V2 plo{}, plr{}, carry{};
-        unsigned mprev = 0;   // fixed mask of row j - 1 (residual mode)
         for (int jb = j0; jb <= j1; jb += D) {
 #pragma unroll
             for (int s = 0; s < D; ++s) {
@@ -690,8 +694,8 @@ __global__ void __launch_bounds__(32 * kMarchWarps) bk_march(BArgs A) {
                     pj.x = fmaf(beta, R.po.x, R.d * M.kdinv[0] * R.r.x);
                     pj.y = fmaf(beta, R.po.y, R.d * M.kdinv[1] * R.r.y);
                 } else {
-                    pj.x = (R.mj & 1u) ? 0.0 : fma(sc, (double)R.xs.x, R.u.x);
-                    pj.y = (R.mj & 2u) ? 0.0 : fma(sc, (double)R.xs.y, R.u.y);
+                    pj.x = fixed ? 0.0 : fma(sc, (double)R.xs.x, R.u.x);
+                    pj.y = fixed ? 0.0 : fma(sc, (double)R.xs.y, R.u.y);
                 }
                 V2 pr;
                 pr.x = __shfl_down_sync(0xffffffffu, pj.x, 1);
@@ -707,13 +711,13 @@ __global__ void __launch_bounds__(32 * kMarchWarps) bk_march(BArgs A) {
                         const T qx = carry.x + y[0][0] + t1x, qy = carry.y + y[1][0] + t1y;
                         const long long n = nb + (long long)nnx * (j - 1);
                         if constexpr (MODE == MV_PCG) {
-                            const float2 qv = make_float2((R.m & 1u) ? 0.f : qx, (R.m & 2u) ? 0.f : qy);
+                            const float2 qv = fixed ? make_float2(0.f, 0.f) : make_float2(qx, qy);
                             reinterpret_cast<float2*>(odd ? A.P1 : A.P0)[n] = plo;
                             reinterpret_cast<float2*>(A.q32)[n] = qv;
                             acc = fmaf(plo.x, qv.x, fmaf(plo.y, qv.y, acc));
                         } else {
-                            const double r0 = (mprev & 1u) ? 0.0 : R.f.x - qx;
-                            const double r1 = (mprev & 2u) ? 0.0 : R.f.y - qy;
+                            const double r0 = fixed ? 0.0 : R.f.x - qx;
+                            const double r1 = fixed ? 0.0 : R.f.y - qy;
                             reinterpret_cast<double2*>(A.r64)[n] = make_double2(r0, r1);
                             acc = fma(r0, r0, fma(r1, r1, acc));
                         }
@@ -723,7 +727,6 @@ __global__ void __launch_bounds__(32 * kMarchWarps) bk_march(BArgs A) {
                 }
                 plo = pj;
                 plr = pr;
-                if constexpr (MODE == MV_RESID) mprev = R.mj;
             }
         }
         const bool last_of_prob = (w + 1 == kend);
@@ -1386,7 +1389,6 @@ int tog_batch_create(int32_t nprob, const int32_t* nelx, const int32_t* nely, co
     auto R = [&](int r) {
         if (rc == TOG_OK) rc = r;
     };
-    uint8_t* fixmask = nullptr;
     double* f = nullptr;
     int* d_soff = nullptr;
     double* d_sw = nullptr;
@@ -1400,7 +1402,6 @@ int tog_batch_create(int32_t nprob, const int32_t* nelx, const int32_t* nely, co
     }
     R(balloc(b, &b->d_nd, b->nd.size()));
     R(balloc(b, &b->d_ce, b->ce.size()));
-    R(balloc(b, &fixmask, NN));
     R(balloc(b, &f, 2 * NN));
     R(balloc(b, &A.u, 2 * NN));
     R(balloc(b, &A.r64, 2 * NN));
@@ -1431,12 +1432,11 @@ int tog_batch_create(int32_t nprob, const int32_t* nelx, const int32_t* nely, co
         bfail(rc, m);
         return rc;
     }
-    // host-side masks and loads: left edge clamped, unit load [0, -1] at (nelx, load_j)
-    std::vector<uint8_t> hm(NN, 0);
+    // loads: unit load [0, -1] at node (nelx, load_j); the clamped left edge is
+    // applied by the operator kernel (nodes of column 0)
     std::vector<double> hf(2 * NN, 0.0);
     for (int p = 0; p < nprob; ++p) {
         const BProb& P = b->probs[p];
-        for (int j = 0; j < P.nn[1]; ++j) hm[P.noff + (long long)P.nn[0] * j] = 3;
         hf[2 * (P.noff + P.nel[0] + (long long)P.nn[0] * load_j[p]) + 1] = -1.0;
     }
     A.P = b->d_P;
@@ -1449,7 +1449,6 @@ int tog_batch_create(int32_t nprob, const int32_t* nelx, const int32_t* nely, co
     A.nprob = nprob;
     A.LY = b->LY;
     std::memcpy(A.Kc, Kc, sizeof(Kc));
-    A.fixmask = fixmask;
     A.f = f;
     A.soff = d_soff;
     A.sw = d_sw;
@@ -1469,7 +1468,6 @@ int tog_batch_create(int32_t nprob, const int32_t* nelx, const int32_t* nely, co
     C(cudaMemcpyAsync(b->d_P, b->probs.data(), nprob * sizeof(BProb), cudaMemcpyHostToDevice, b->own));
     C(cudaMemcpyAsync(b->d_nd, b->nd.data(), b->nd.size() * sizeof(Item), cudaMemcpyHostToDevice, b->own));
     C(cudaMemcpyAsync(b->d_ce, b->ce.data(), b->ce.size() * sizeof(Item), cudaMemcpyHostToDevice, b->own));
-    C(cudaMemcpyAsync(fixmask, hm.data(), NN, cudaMemcpyHostToDevice, b->own));
     C(cudaMemcpyAsync(f, hf.data(), 2 * NN * sizeof(double), cudaMemcpyHostToDevice, b->own));
     C(cudaMemcpyAsync(d_soff, soff.data(), soff.size() * sizeof(int), cudaMemcpyHostToDevice, b->own));
     C(cudaMemcpyAsync(d_sw, sw.data(), sw.size() * sizeof(double), cudaMemcpyHostToDevice, b->own));
