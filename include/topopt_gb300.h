@@ -40,6 +40,9 @@ enum tog_precision {
 };
 
 enum tog_filter_kind { TOG_FILTER_NONE = 0, TOG_FILTER_DENSITY = 1, TOG_FILTER_SENS = 2 };
+/* warm_start of tog_simp_step: 0 cold, 1 previous displacement, TOG_WARM_LEARNED the
+ * previous displacement moved along the attached network's correction (3D). */
+enum tog_warm_start { TOG_WARM_COLD = 0, TOG_WARM_PREVIOUS = 1, TOG_WARM_LEARNED = 2 };
 enum tog_filter_op { TOG_FILTER_J = 0, TOG_FILTER_JT = 1 };
 
 typedef struct tog_handle tog_handle;
@@ -148,8 +151,8 @@ int tog_oc_update(tog_handle* h, const double* x, const double* dc, const double
  * docs/tutorials/simp.qmd:86-114 with OC in place of MMA. */
 /* filter_kind: TOG_FILTER_NONE / DENSITY / SENS (needs rmin > 0). x0: initial design. */
 int tog_simp_init(tog_handle* h, int32_t filter_kind, double rmin, double volfrac, double move, const double* x0);
-/* precision: TOG_FP64 (cold start, as the reference) or TOG_FP32_IR; warm_start != 0
- * starts each solve from the previous displacement. */
+/* precision: TOG_FP64 (cold start, as the reference) or TOG_FP32_IR; warm_start: see
+ * tog_warm_start (nonzero starts each solve from the previous displacement). */
 int tog_simp_step(tog_handle* h, int32_t precision, double rtol, int32_t maxiter, int32_t warm_start,
                   tog_iter_stats* stats);
 int tog_get_design(tog_handle* h, double* x);
@@ -205,6 +208,43 @@ int tog_batch_solve_info(tog_batch* b, double* residual, int32_t* refreshes, int
 int tog_batch_bench_kernel(tog_batch* b, int32_t kernel, int32_t nlaunch, double* us_per_launch);
 /* Algorithmic HBM bytes of one launch of that kernel over all problems. */
 int tog_batch_kernel_bytes(tog_batch* b, int32_t kernel, double* bytes);
+
+/* ---- learned warm start (no counterpart in TopOpt.jl) -----------------------------------
+ * A 3D convolutional encoder-decoder (4 levels, 16/32/48/64 channels, 3x3x3 kernels, BF16
+ * weights and activations with FP32 accumulation on the tensor cores) for a structured
+ * node grid of nodes[0] x nodes[1] x nodes[2] (x fastest), trained and evaluated on the
+ * GPU by the library's own kernels.  Tensors are FP32, channels-last, on the device:
+ * input batch x nodes x 8 (new filtered density, its change, previous displacement /
+ * scale (3), load / max |load| (3); densities averaged from the cells to the nodes),
+ * output / target batch x nodes x 3 (displacement correction / scale).  Parameters are
+ * one FP32 vector: per layer W[cout][27][cin] then b[cout]. */
+typedef struct tog_nn tog_nn;
+int tog_nn_create(const int32_t nodes[3], int32_t batch, uint64_t seed, tog_nn** out);
+int tog_nn_destroy(tog_nn* nn);
+int tog_nn_set_stream(tog_nn* nn, void* stream);
+int tog_nn_param_count(const tog_nn* nn, int64_t* count);
+int tog_nn_get_params(tog_nn* nn, float* params);
+/* Also resets the optimiser state. */
+int tog_nn_set_params(tog_nn* nn, const float* params);
+int tog_nn_forward(tog_nn* nn, const float* in_dev, float* out_dev);
+/* Mean squared error against target_dev and its gradient w.r.t. every parameter (host
+ * vector of tog_nn_param_count floats; may be NULL); no update. */
+int tog_nn_gradients(tog_nn* nn, const float* in_dev, const float* target_dev, double* loss, float* grads);
+/* One Adam step (beta 0.9 / 0.999) on the mean squared error; loss may be NULL. */
+int tog_nn_train_step(tog_nn* nn, const float* in_dev, const float* target_dev, float lr, double* loss);
+/* Attach (or, with NULL, detach) a network to a 3D solver handle; it must have been created for
+ * the handle's node grid with batch 1.  tog_simp_step with warm_start = TOG_WARM_LEARNED then
+ * builds the network input from the handle's state on the device, runs the network and moves
+ * the previous displacement u along its correction d by the Galerkin step alpha = d.r0 / d.Kd
+ * (r0 = f - K u), which never increases the energy norm of the error; the PCG solve then
+ * finishes to the requested tolerance as before.  The first design iteration (no previous
+ * state) falls back to the previous-displacement start. */
+int tog_set_warm_start_net(tog_handle* h, tog_nn* nn);
+/* Training data: the next tog_simp_step writes its network input (nodes x 8) and target (the
+ * solve's displacement change / max |u_prev|, nodes x 3) into these FP32 device buffers, if it
+ * has a previous iteration; tog_record_status reports whether it did (written = 1). */
+int tog_record_next_step(tog_handle* h, float* input_dev, float* target_dev);
+int tog_record_status(tog_handle* h, int32_t* written);
 
 /* ---- allocation-free OC update: no counterpart in TopOpt.jl ----------------------------
  * For callers that cannot call cudaMalloc (a framework that owns and pre-partitions all

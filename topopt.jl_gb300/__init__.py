@@ -15,12 +15,14 @@ from .topopt_api import (  # noqa: F401
     GB300FEASolver,
     GB300Solver,
     HalfMBB,
+    LoadedCantilever,
     PointLoadCantilever,
     PowerPenaltyFun,
     PseudoDensities,
     SensFilterFun,
     SIMPLoop,
     VolumeFun,
+    WarmStartNet,
     cell_dofs,
     config3_problems,
     element_stiffness,

@@ -84,6 +84,18 @@ SIGNATURES = {
     "tog_batch_solve_info": (C.c_int, [_H, _D, _I32, _I32]),
     "tog_batch_bench_kernel": (C.c_int, [_H, C.c_int32, C.c_int32, C.POINTER(C.c_double)]),
     "tog_batch_kernel_bytes": (C.c_int, [_H, C.c_int32, C.POINTER(C.c_double)]),
+    "tog_nn_create": (C.c_int, [C.POINTER(C.c_int32), C.c_int32, C.c_uint64, C.POINTER(C.c_void_p)]),
+    "tog_nn_destroy": (C.c_int, [_H]),
+    "tog_nn_set_stream": (C.c_int, [_H, C.c_void_p]),
+    "tog_nn_param_count": (C.c_int, [_H, C.POINTER(C.c_int64)]),
+    "tog_nn_get_params": (C.c_int, [_H, C.POINTER(C.c_float)]),
+    "tog_nn_set_params": (C.c_int, [_H, C.POINTER(C.c_float)]),
+    "tog_nn_forward": (C.c_int, [_H, C.c_void_p, C.c_void_p]),
+    "tog_nn_gradients": (C.c_int, [_H, C.c_void_p, C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_float)]),
+    "tog_nn_train_step": (C.c_int, [_H, C.c_void_p, C.c_void_p, C.c_float, C.POINTER(C.c_double)]),
+    "tog_set_warm_start_net": (C.c_int, [_H, _H]),
+    "tog_record_next_step": (C.c_int, [_H, C.c_void_p, C.c_void_p]),
+    "tog_record_status": (C.c_int, [_H, _I32]),
     "tog_oc_update_noalloc": (C.c_int, [C.c_int64, _D, _D, _D, _D, C.c_double, C.c_double, _D, _D, C.c_void_p]),
 }
 

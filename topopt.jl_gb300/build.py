@@ -35,6 +35,8 @@ def build(verbose=False):
                                   "-o", os.path.join(BUILD, "tog_batch.o")],
         [NVCC] + COMMON + ARCH + ["-lineinfo", "-c", os.path.join(CSRC, "tog_noalloc.cu"),
                                   "-o", os.path.join(BUILD, "tog_noalloc.o")],
+        [NVCC] + COMMON + ARCH + ["-lineinfo", "-c", os.path.join(CSRC, "tog_nn.cu"),
+                                  "-o", os.path.join(BUILD, "tog_nn.o")],
         [NVCC] + COMMON + ["-x", "c++", "-c", os.path.join(CSRC, "tog_host.cpp"),
                            "-o", os.path.join(BUILD, "tog_host.o")],
     ]
@@ -42,7 +44,8 @@ def build(verbose=False):
         logs = list(ex.map(_run, jobs))
     tmp = LIB + ".tmp"
     _run([NVCC] + ARCH + ["-shared", "-o", tmp, os.path.join(BUILD, "tog_api.o"), os.path.join(BUILD, "tog_batch.o"),
-                          os.path.join(BUILD, "tog_noalloc.o"), os.path.join(BUILD, "tog_host.o")])
+                          os.path.join(BUILD, "tog_noalloc.o"), os.path.join(BUILD, "tog_nn.o"),
+                          os.path.join(BUILD, "tog_host.o")])
     os.replace(tmp, LIB)
     if verbose:
         print("".join(logs))

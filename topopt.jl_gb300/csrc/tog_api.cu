@@ -13,6 +13,7 @@
 
 #include "../../include/topopt_gb300.h"
 #include "tog_host.h"
+#include "tog_nn.h"
 #include "tog_kernels.cuh"
 #include "tog_mv3.cuh"
 #include "tog_mv3x2.cuh"
@@ -115,6 +116,18 @@ struct tog_handle {
     double *d_x = nullptr, *d_xnew = nullptr, *d_dc = nullptr, *d_dv = nullptr, *d_w = nullptr, *d_grad = nullptr,
            *d_B = nullptr;
     bool simp_ready = false;
+    // learned warm start (3D): network, previous-iteration state and recording hook
+    tog_nn* net = nullptr;
+    double* d_vars_prev = nullptr;   // physical densities of the previous design iteration
+    double* d_uprev = nullptr;       // displacement before the solve (recording)
+    float* d_nn_in = nullptr;        // network input (nodes x 8)
+    float* d_nn_out = nullptr;       // network output (nodes x 3)
+    double* d_nn_sc = nullptr;       // max |u|, max |f|, step length alpha
+    double* d_nn_part = nullptr;
+    unsigned* d_nn_cnt = nullptr;
+    bool have_prev = false;
+    float *rec_in = nullptr, *rec_tgt = nullptr;
+    int rec_written = 0;
     // 3D operator tiling: tiles of 32 x MV3_BY elements, LZ layers per z chunk
     int nt[3] = {1, 1, 1};
     int LZ = 8;
@@ -558,6 +571,144 @@ int solve_fp32_ir(tog_handle* h, double rtol, double abstol, int maxit, int warm
     return TOG_OK;
 }
 
+// ---------------------------------------------------------------------------
+// learned warm start (3D structured grids; no counterpart in TopOpt.jl)
+// ---------------------------------------------------------------------------
+constexpr int kNnBlocks = 1024;   // grid of the warm-start reductions (partials sized for it)
+
+// sc[0] = max |u| (1 when zero), sc[1] = max |f| (1 when zero)
+__global__ void k_nn_scales(const double* __restrict__ u, const double* __restrict__ f, long long n,
+                            double* partials, unsigned* cnt, double* sc) {
+    double v[2] = {0.0, 0.0};
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        v[0] = fmax(v[0], fabs(u[i]));
+        v[1] = fmax(v[1], fabs(f[i]));
+    }
+    double tot[2];
+    if (grid_reduce_last<2, true>(v, partials, cnt, tot) && threadIdx.x == 0) {
+        sc[0] = tot[0] > 0.0 ? tot[0] : 1.0;
+        sc[1] = tot[1] > 0.0 ? tot[1] : 1.0;
+    }
+}
+
+// network input per node: mean of the adjacent cells' new physical density and of
+// its change, u / max|u| and f / max|f| (internal AoS dof layout 3 n + c)
+__global__ void k_nn_input(Dims D, const double* __restrict__ vars, const double* __restrict__ prev,
+                           const double* __restrict__ u, const double* __restrict__ f, const double* __restrict__ sc,
+                           float* __restrict__ out) {
+    const double iu = 1.0 / sc[0], iff = 1.0 / sc[1];
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < D.nnodes;
+         n += (long long)gridDim.x * blockDim.x) {
+        const int ix = (int)(n % D.nn[0]), iy = (int)((n / D.nn[0]) % D.nn[1]), iz = (int)(n / ((long long)D.nn[0] * D.nn[1]));
+        double s = 0.0, ds = 0.0;
+        int c = 0;
+        for (int dz = -1; dz <= 0; ++dz)
+            for (int dy = -1; dy <= 0; ++dy)
+                for (int dx = -1; dx <= 0; ++dx) {
+                    const int cx = ix + dx, cy = iy + dy, cz = iz + dz;
+                    if (cx < 0 || cy < 0 || cz < 0 || cx >= D.nel[0] || cy >= D.nel[1] || cz >= D.nel[2]) continue;
+                    const long long e = cx + (long long)D.nel[0] * (cy + (long long)D.nel[1] * cz);
+                    s += vars[e];
+                    ds += vars[e] - prev[e];
+                    ++c;
+                }
+        float* o = out + 8 * n;
+        o[0] = (float)(s / c);
+        o[1] = (float)(ds / c);
+        for (int k = 0; k < 3; ++k) {
+            o[2 + k] = (float)(u[3 * n + k] * iu);
+            o[5 + k] = (float)(f[3 * n + k] * iff);
+        }
+    }
+}
+
+// correction direction d = max|u| * network output, zero at fixed dofs
+__global__ void k_nn_direction(const float* __restrict__ y, const uint8_t* __restrict__ fixmask,
+                               const double* __restrict__ sc, double* __restrict__ d, long long nnodes) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < 3 * nnodes;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long n = i / 3;
+        const int c = (int)(i - 3 * n);
+        d[i] = ((fixmask[n] >> c) & 1u) ? 0.0 : sc[0] * (double)y[i];
+    }
+}
+
+// Galerkin step length along d: alpha = d.r0 / d.Kd (0 unless d.Kd > 0), sc[2]
+__global__ void k_nn_alpha(const double* __restrict__ d, const double* __restrict__ r0, const double* __restrict__ kd,
+                           long long n, double* partials, unsigned* cnt, double* sc) {
+    double v[2] = {0.0, 0.0};
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        v[0] = fma(d[i], r0[i], v[0]);
+        v[1] = fma(d[i], kd[i], v[1]);
+    }
+    double tot[2];
+    if (grid_reduce_last<2>(v, partials, cnt, tot) && threadIdx.x == 0)
+        sc[2] = (tot[1] > 0.0 && isfinite(tot[0] / tot[1])) ? tot[0] / tot[1] : 0.0;
+}
+
+__global__ void k_nn_step(double* __restrict__ u, const double* __restrict__ d, const double* __restrict__ sc,
+                          long long n) {
+    const double a = sc[2];
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        u[i] = fma(a, d[i], u[i]);
+}
+
+// training target: (u_new - u_prev) / max|u_prev|
+__global__ void k_nn_target(const double* __restrict__ u, const double* __restrict__ uprev,
+                            const double* __restrict__ sc, float* __restrict__ tgt, long long n) {
+    const double iu = 1.0 / sc[0];
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        tgt[i] = (float)((u[i] - uprev[i]) * iu);
+}
+
+int nn_buffers(tog_handle* h) {
+    if (h->d_vars_prev) return TOG_OK;
+    int rc = TOG_OK;
+    auto A = [&](int r) {
+        if (rc == TOG_OK) rc = r;
+    };
+    A(dalloc(&h->d_vars_prev, h->ncells));
+    A(dalloc(&h->d_uprev, h->ndofs));
+    A(dalloc(&h->d_nn_in, 8 * h->nnodes));
+    A(dalloc(&h->d_nn_out, 3 * h->nnodes));
+    A(dalloc(&h->d_nn_sc, 4));
+    A(dalloc(&h->d_nn_part, 2 * kNnBlocks));
+    A(dalloc(&h->d_nn_cnt, 4));
+    if (rc != TOG_OK) return rc;
+    TOG_CUDA(cudaMemsetAsync(h->d_nn_cnt, 0, 4 * sizeof(unsigned), h->stream));
+    h->have_prev = false;
+    return TOG_OK;
+}
+
+// Before the solve of a design iteration (new physical densities in d_vars, the
+// previous solution in d_u): write the network input (into the recording buffer
+// when one is set) and, with a network attached and apply set, move d_u along the
+// network's correction by the Galerkin step, which never increases the energy
+// norm of the error.
+int nn_before_solve(tog_handle* h, bool apply) {
+    cudaStream_t s = h->stream;
+    const int nb = (int)std::min<long long>(kNnBlocks, h->ew_blocks(h->ndofs));
+    k_nn_scales<<<nb, kEwThreads, 0, s>>>(h->d_u, h->d_f, h->ndofs, h->d_nn_part, h->d_nn_cnt, h->d_nn_sc);
+    float* in = h->rec_in ? h->rec_in : h->d_nn_in;
+    k_nn_input<<<h->ew_blocks(h->nnodes), kEwThreads, 0, s>>>(h->dims(), h->d_vars, h->d_vars_prev, h->d_u, h->d_f,
+                                                             h->d_nn_sc, in);
+    if (h->rec_in)
+        TOG_CUDA(cudaMemcpyAsync(h->d_uprev, h->d_u, h->ndofs * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    if (apply) {
+        TOG_TRY(refresh_scales(h));
+        TOG_TRY(nn_forward_dev(h->net, in, h->d_nn_out, s));
+        k_nn_direction<<<h->ew_blocks(h->ndofs), kEwThreads, 0, s>>>(h->d_nn_out, h->d_fixmask, h->d_nn_sc, h->d_tmp,
+                                                                   h->nnodes);
+        launch_matvec<double, MV_RESID>(h, s, h->d_u, h->d_r64, h->d_f);       // r0 = f - K u
+        launch_matvec<double, MV_PLAIN>(h, s, h->d_tmp, h->d_q64, nullptr);    // K d
+        k_nn_alpha<<<nb, kEwThreads, 0, s>>>(h->d_tmp, h->d_r64, h->d_q64, h->ndofs, h->d_nn_part, h->d_nn_cnt + 1,
+                                             h->d_nn_sc);
+        k_nn_step<<<h->ew_blocks(h->ndofs), kEwThreads, 0, s>>>(h->d_u, h->d_tmp, h->d_nn_sc, h->ndofs);
+    }
+    TOG_CUDA(cudaGetLastError());
+    return TOG_OK;
+}
+
 int do_solve(tog_handle* h, int prec, double rtol, double abstol, int maxit, int warm, tog_solve_stats* st) {
     TOG_TRY(refresh_scales(h));
     if (prec == TOG_FP64) return solve_fp64(h, rtol, abstol, maxit, warm, st);
@@ -926,7 +1077,8 @@ int tog_destroy(tog_handle* h) {
     void* ptrs[] = {h->d_int2ref, h->d_ref2int, h->d_fixmask, h->d_vecpool, h->d_vars,    h->d_e64,
                     h->d_e32,     h->d_dinv64,  h->d_dinv32,  h->d_nodal,   h->d_st64,    h->d_st32,
                     h->d_oc,      h->d_partials, h->d_cnt,    h->d_scalar,  h->d_invW,    h->d_soff,
-                    h->d_sw};
+                    h->d_sw,      h->d_vars_prev, h->d_uprev, h->d_nn_in, h->d_nn_out, h->d_nn_sc,
+                    h->d_nn_part, h->d_nn_cnt};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (int i = 0; i < 6; ++i)
@@ -1152,9 +1304,26 @@ int tog_simp_step(tog_handle* h, int32_t precision, double rtol, int32_t maxiter
     else
         TOG_CUDA(cudaMemcpyAsync(h->d_vars, h->d_x, bytes, cudaMemcpyDeviceToDevice, h->stream));
     h->vars_dirty = true;
+    // learned warm start / recording: need the previous iteration's densities and solution
+    const bool prev_ok = h->d_vars_prev && h->have_prev && h->u_valid && h->dim == 3;
+    const bool learned = warm_start == TOG_WARM_LEARNED && h->net && prev_ok;
+    const bool record = h->rec_in && prev_ok;
+    if (!record) h->rec_in = nullptr;
+    if (learned || record) TOG_TRY(nn_before_solve(h, learned));
     tog_solve_stats ss{};
-    int rc = do_solve(h, precision, rtol, 0.0, maxiter, warm_start, &ss);
+    int rc = do_solve(h, precision, rtol, 0.0, maxiter, warm_start != 0, &ss);
     if (rc != TOG_OK && rc != TOG_NOT_CONVERGED) return rc;
+    if (record) {
+        k_nn_target<<<h->ew_blocks(h->ndofs), kEwThreads, 0, h->stream>>>(h->d_u, h->d_uprev, h->d_nn_sc, h->rec_tgt,
+                                                                         h->ndofs);
+        h->rec_written = 1;
+    }
+    h->rec_in = nullptr;
+    h->rec_tgt = nullptr;
+    if (h->d_vars_prev) {
+        TOG_CUDA(cudaMemcpyAsync(h->d_vars_prev, h->d_vars, bytes, cudaMemcpyDeviceToDevice, h->stream));
+        h->have_prev = true;
+    }
     TOG_TRY(compliance_dev(h, h->d_grad));
     if (h->simp_filter == TOG_FILTER_DENSITY)
         TOG_TRY(filter_dev(h, TOG_FILTER_JT, h->d_grad, h->d_dc));
@@ -1179,6 +1348,37 @@ int tog_simp_step(tog_handle* h, int32_t precision, double rtol, int32_t maxiter
         stats->rel_residual = ss.rel_residual;
     }
     return rc;
+}
+
+int tog_set_warm_start_net(tog_handle* h, tog_nn* nn) {
+    TOG_TRY(check_handle(h));
+    if (nn) {
+        if (h->dim != 3) return fail(TOG_ERR_ARG, "the learned warm start is for 3D grids");
+        const int nodes[3] = {h->nn[0], h->nn[1], h->nn[2]};
+        if (!nn_matches(nn, nodes, 1))
+            return fail(TOG_ERR_ARG, "network created for another node grid (or a batch other than 1)");
+        TOG_TRY(nn_buffers(h));
+    }
+    h->net = nn;
+    return TOG_OK;
+}
+
+int tog_record_next_step(tog_handle* h, float* input_dev, float* target_dev) {
+    TOG_TRY(check_handle(h));
+    if (!input_dev || !target_dev) return fail(TOG_ERR_ARG, "null recording buffer");
+    if (h->dim != 3) return fail(TOG_ERR_ARG, "recording is for 3D grids");
+    TOG_TRY(nn_buffers(h));
+    h->rec_in = input_dev;
+    h->rec_tgt = target_dev;
+    h->rec_written = 0;
+    return TOG_OK;
+}
+
+int tog_record_status(tog_handle* h, int32_t* written) {
+    TOG_TRY(check_handle(h));
+    if (!written) return fail(TOG_ERR_ARG, "null output");
+    *written = h->rec_written;
+    return TOG_OK;
 }
 
 int tog_get_design(tog_handle* h, double* x) {

@@ -103,6 +103,28 @@ class PointLoadCantilever(_StructuredProblem):
         self.force_dof = int(self.node_dofs[self.load_node, 1])
 
 
+class LoadedCantilever(_StructuredProblem):
+    """3D cantilever with the left face clamped and a point load of magnitude `force` in
+    direction `direction` at the node (nelx, iy, iz) of the free face (the training runs of
+    the learned warm start; PointLoadCantilever is the case iy = nely / 2, iz = 0,
+    direction -y)."""
+
+    def __init__(self, nels, sizes, node, direction, E=1.0, nu=0.3, force=1.0):
+        super().__init__(nels, sizes, E, nu, force, False)
+        if self.dim != 3:
+            raise ValueError("LoadedCantilever is 3D")
+        ix, iy, iz = self._node_grid()
+        self.fixed_dofs = np.sort(self.node_dofs[np.nonzero(ix == 0)[0]].ravel()).astype(np.int32)
+        self.load_node = self.node_id(self.nels[0], int(node[0]), int(node[1]))
+        d = np.asarray(direction, dtype=np.float64)
+        self.direction = d / np.linalg.norm(d)
+
+    def load_vector(self):
+        f = np.zeros(self.ndofs)
+        f[self.node_dofs[self.load_node]] = self.force * self.direction
+        return f
+
+
 class HalfMBB(_StructuredProblem):
     """u1 = 0 on the left face, u2 = 0 on bottom & right, load [0, -force] at the
     first node of top & left (problem_types.jl:324-395)."""
@@ -134,6 +156,7 @@ class GB300Solver:
 
 
 PRECISIONS = {"fp64": L.TOG_FP64, "fp32_ir": L.TOG_FP32_IR}
+WARM_MODES = {False: 0, True: 1, 0: 0, 1: 1, 2: 2, "cold": 0, "previous": 1, "learned": 2}
 
 
 class GB300FEASolver:
@@ -152,7 +175,10 @@ class GB300FEASolver:
         if precision not in PRECISIONS:
             raise ValueError("precision must be one of %s" % sorted(PRECISIONS))
         self.precision = precision
-        self.warm_start = bool(warm_start)
+        # False / True (previous displacement) / "learned" (previous displacement moved
+        # along an attached WarmStartNet's correction; SIMP steps of 3D problems)
+        self.warm_start = WARM_MODES[warm_start]
+        self.net = None
         d = L.ProblemDesc()
         d.dim = problem.dim
         for i in range(problem.dim):
@@ -182,6 +208,22 @@ class GB300FEASolver:
         except Exception:
             pass
 
+    def attach_network(self, net):
+        """Use a WarmStartNet (created for this grid's nodes, batch 1) for warm_start="learned"."""
+        L.check(L.lib().tog_set_warm_start_net(self.handle, net.handle if net is not None else None))
+        self.net = net
+
+    def record_next_step(self, inp, target):
+        """The next SIMP step writes its network input / target into these CUDA tensors
+        (shapes (1, nz, ny, nx, 8) and (1, nz, ny, nx, 3)) when it has a previous iteration."""
+        L.check(L.lib().tog_record_next_step(self.handle, L.C.c_void_p(inp.data_ptr()),
+                                             L.C.c_void_p(target.data_ptr())))
+
+    def record_status(self):
+        w = L.C.c_int32()
+        L.check(L.lib().tog_record_status(self.handle, L.C.byref(w)))
+        return bool(w.value)
+
     def setpenalty(self, p):
         self.penalty = p if isinstance(p, PowerPenaltyFun) else PowerPenaltyFun(p)
         L.check(L.lib().tog_set_penalty(self.handle, self.penalty.p))
@@ -197,7 +239,7 @@ class GB300FEASolver:
         self._push_vars()
         st = L.SolveStats()
         prec = PRECISIONS[precision or self.precision]
-        warm = self.warm_start if warm_start is None else warm_start
+        warm = self.warm_start if warm_start is None else WARM_MODES[warm_start]
         L.check(L.lib().tog_solve(self.handle, prec, self.rtol, self.abstol, self.cg_max_iter, int(warm),
                                   L.C.byref(st)))
         self.last_stats = st
@@ -345,7 +387,8 @@ class SIMPLoop:
         code = L.lib().tog_simp_step(s.handle, PRECISIONS[precision or s.precision],
                                      s.rtol if rtol is None else float(rtol),
                                      s.cg_max_iter if maxiter is None else int(maxiter),
-                                     int(s.warm_start if warm_start is None else warm_start), L.C.byref(st))
+                                     s.warm_start if warm_start is None else WARM_MODES[warm_start],
+                                     L.C.byref(st))
         L.check(code)
         return st
 
@@ -461,3 +504,75 @@ class BatchedSIMP:
         L.check(L.lib().tog_batch_bench_kernel(self.handle, int(kernel), int(nlaunch), L.C.byref(us)))
         L.check(L.lib().tog_batch_kernel_bytes(self.handle, int(kernel), L.C.byref(by)))
         return us.value, by.value
+
+
+# --------------------------------------------------------------------------- learned warm start
+class WarmStartNet:
+    """The learned warm-start network of libtopopt_gb300 (tog_nn_*): a 3D
+    convolutional encoder-decoder on a structured node grid, trained and run by
+    the library's tensor-core kernels.  Tensors are CUDA float32 torch tensors,
+    channels-last: inputs (batch, nz, ny, nx, 8), outputs / targets (batch, nz,
+    ny, nx, 3)."""
+
+    def __init__(self, nodes, batch=1, seed=0):
+        self.nodes = tuple(int(n) for n in nodes)
+        self.batch = int(batch)
+        h = L.C.c_void_p()
+        nn = (L.C.c_int32 * 3)(*self.nodes)
+        L.check(L.lib().tog_nn_create(nn, self.batch, int(seed), L.C.byref(h)))
+        self.handle = h
+        c = L.C.c_int64()
+        L.check(L.lib().tog_nn_param_count(h, L.C.byref(c)))
+        self.n_params = c.value
+
+    def close(self):
+        if getattr(self, "handle", None):
+            L.lib().tog_nn_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_ptr):
+        L.check(L.lib().tog_nn_set_stream(self.handle, L.C.c_void_p(stream_ptr)))
+
+    def get_params(self):
+        p = np.empty(self.n_params, dtype=np.float32)
+        L.check(L.lib().tog_nn_get_params(self.handle, p.ctypes.data_as(L.C.POINTER(L.C.c_float))))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        assert p.size == self.n_params
+        L.check(L.lib().tog_nn_set_params(self.handle, p.ctypes.data_as(L.C.POINTER(L.C.c_float))))
+
+    def _shape(self, t, c):
+        nx, ny, nz = self.nodes
+        if tuple(t.shape) != (self.batch, nz, ny, nx, c) or not t.is_cuda or not t.is_contiguous():
+            raise ValueError("expected a contiguous CUDA tensor of shape %s" % ((self.batch, nz, ny, nx, c),))
+
+    def forward(self, inp, out=None):
+        import torch
+        self._shape(inp, 8)
+        if out is None:
+            out = torch.empty(inp.shape[:-1] + (3,), dtype=torch.float32, device=inp.device)
+        L.check(L.lib().tog_nn_forward(self.handle, L.C.c_void_p(inp.data_ptr()), L.C.c_void_p(out.data_ptr())))
+        return out
+
+    def gradients(self, inp, target):
+        self._shape(inp, 8)
+        self._shape(target, 3)
+        g = np.empty(self.n_params, dtype=np.float32)
+        loss = L.C.c_double()
+        L.check(L.lib().tog_nn_gradients(self.handle, L.C.c_void_p(inp.data_ptr()), L.C.c_void_p(target.data_ptr()),
+                                         L.C.byref(loss), g.ctypes.data_as(L.C.POINTER(L.C.c_float))))
+        return loss.value, g
+
+    def train_step(self, inp, target, lr=1e-3):
+        loss = L.C.c_double()
+        L.check(L.lib().tog_nn_train_step(self.handle, L.C.c_void_p(inp.data_ptr()), L.C.c_void_p(target.data_ptr()),
+                                          float(lr), L.C.byref(loss)))
+        return loss.value
