@@ -225,6 +225,39 @@ def batch_leg(tg, stream, peaks, src, steps):
     return out
 
 
+WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "topopt.jl_gb300", "weights",
+                       "warmstart_96x48x48.npy")
+
+
+def learned_leg(tg, steps):
+    """Learned warm start: 3D cantilever 96x48x48, one held-out seeded run (volume
+    fraction, load node on the free face and direction drawn from seed 1000), the same
+    trajectory solved with a cold, a previous-step and a learned start (network trained
+    by topopt.jl_gb300/learned.py on seeded runs of the same grid, weights committed)."""
+    if not os.path.exists(WEIGHTS):
+        return {"unavailable": "no trained weights at topopt.jl_gb300/weights/"}
+    from topopt_gb300 import learned as LW
+    nels = (96, 48, 48)
+    net = tg.WarmStartNet(tuple(n + 1 for n in nels), batch=1, seed=0)
+    net.set_params(np.load(WEIGHTS))
+    run = LW.sample_runs(1, nels, seed=1000)[0]
+    ev = LW.evaluate(nels, run, steps, net)
+    net.close()
+    prev = ev["previous"]
+    out = {"workload": "3D cantilever 96x48x48, held-out run %s" % json.dumps(
+        {"volfrac": round(run["volfrac"], 4), "node": run["node"],
+         "direction": [round(float(v), 4) for v in run["direction"]]}),
+           "design_iters": steps, "rtol": 1e-8}
+    for m, r in ev.items():
+        out[m] = {"cg_iters_mean": r["cg_iters_mean"], "s_per_design_iter": r["s_per_iter"],
+                  "cg_iters": r["cg_iters"]}
+    out["learned_vs_previous_cg"] = ev["learned"]["cg_iters_mean"] / prev["cg_iters_mean"]
+    out["learned_vs_cold_cg"] = ev["learned"]["cg_iters_mean"] / ev["cold"]["cg_iters_mean"]
+    out["compliance_spread_last"] = float(np.ptp([r["compliance"][-1] for r in ev.values()]) /
+                                          abs(prev["compliance"][-1]))
+    return out
+
+
 def run_ours(args):
     import torch
     ws, rank, local = dist_setup()
@@ -359,6 +392,7 @@ def run_ours(args):
                            "achieved_gbs": ubytes / t_u / 1e9, "frac": ubytes / t_u / 1e9 / peaks["hbm_gbs"]}}
     solver.close()
     batched = batch_leg(tg, stream, peaks, src, int(os.environ.get("BATCH_STEPS", "3")))
+    learned = learned_leg(tg, int(os.environ.get("LEARNED_STEPS", "12")))
 
     cg = [int(s.cg_iterations) for s in stats]
     line = {"metric": METRIC, "value": value, "unit": "design_iters/s", "n_gpus": ws, "steps": args.steps,
@@ -369,7 +403,7 @@ def run_ours(args):
                        "l2": "working set ~0.3 GB per GPU > 129 MB L2 (no flush)",
                        "parallelism": "replicas" if ws > 1 else "single GPU"},
             "clocks": clocks, "e2e": e2e, "gpu_launches": int(launches), "roofline": roof,
-            "fp64_pcg": fp64, "accuracy_vs_fp64": acc, "batched_2d": batched,
+            "fp64_pcg": fp64, "accuracy_vs_fp64": acc, "batched_2d": batched, "learned_warm_start": learned,
             "inner_cg_iters_per_step": cg,
             "outer_iters_per_step": [int(s.outer_iterations) for s in stats],
             "compliance_last": stats[-1].compliance}

@@ -40,9 +40,12 @@ enum tog_precision {
 };
 
 enum tog_filter_kind { TOG_FILTER_NONE = 0, TOG_FILTER_DENSITY = 1, TOG_FILTER_SENS = 2 };
-/* warm_start of tog_simp_step: 0 cold, 1 previous displacement, TOG_WARM_LEARNED the
- * previous displacement moved along the attached network's correction (3D). */
-enum tog_warm_start { TOG_WARM_COLD = 0, TOG_WARM_PREVIOUS = 1, TOG_WARM_LEARNED = 2 };
+/* warm_start of tog_simp_step: 0 cold, 1 previous displacement; for 3D handles with
+ * tog_set_warm_start_net / tog_record_next_step buffers also TOG_WARM_LEARNED (the previous
+ * displacement moved by the Galerkin step on span{network correction, last displacement
+ * change}) and TOG_WARM_EXTRAPOLATE (the same step along the last change alone, the ablation
+ * without the network). */
+enum tog_warm_start { TOG_WARM_COLD = 0, TOG_WARM_PREVIOUS = 1, TOG_WARM_LEARNED = 2, TOG_WARM_EXTRAPOLATE = 3 };
 enum tog_filter_op { TOG_FILTER_J = 0, TOG_FILTER_JT = 1 };
 
 typedef struct tog_handle tog_handle;
@@ -215,7 +218,8 @@ int tog_batch_kernel_bytes(tog_batch* b, int32_t kernel, double* bytes);
  * node grid of nodes[0] x nodes[1] x nodes[2] (x fastest), trained and evaluated on the
  * GPU by the library's own kernels.  Tensors are FP32, channels-last, on the device:
  * input batch x nodes x 8 (new filtered density, its change, previous displacement /
- * scale (3), load / max |load| (3); densities averaged from the cells to the nodes),
+ * max |u| (3), residual f - K(new densities) u / max |residual| (3); densities averaged
+ * from the cells to the nodes),
  * output / target batch x nodes x 3 (displacement correction / scale).  Parameters are
  * one FP32 vector: per layer W[cout][27][cin] then b[cout]. */
 typedef struct tog_nn tog_nn;
@@ -235,14 +239,18 @@ int tog_nn_train_step(tog_nn* nn, const float* in_dev, const float* target_dev, 
 /* Attach (or, with NULL, detach) a network to a 3D solver handle; it must have been created for
  * the handle's node grid with batch 1.  tog_simp_step with warm_start = TOG_WARM_LEARNED then
  * builds the network input from the handle's state on the device, runs the network and moves
- * the previous displacement u along its correction d by the Galerkin step alpha = d.r0 / d.Kd
- * (r0 = f - K u), which never increases the energy norm of the error; the PCG solve then
- * finishes to the requested tolerance as before.  The first design iteration (no previous
- * state) falls back to the previous-displacement start. */
+ * the previous displacement u by the Galerkin step on span{d, du} (d the network's correction,
+ * du the previous iteration's displacement change, r0 = f - K u), which never increases the
+ * energy norm of the error; the PCG solve then finishes to the requested tolerance as before.
+ * Without a previous state (first design iteration) the start is the previous displacement. */
 int tog_set_warm_start_net(tog_handle* h, tog_nn* nn);
+/* Keep the previous design iteration's state on the device (densities, displacement, its last
+ * change) so that TOG_WARM_EXTRAPOLATE can be used without a network (3D). */
+int tog_keep_previous_state(tog_handle* h);
 /* Training data: the next tog_simp_step writes its network input (nodes x 8) and target (the
- * solve's displacement change / max |u_prev|, nodes x 3) into these FP32 device buffers, if it
- * has a previous iteration; tog_record_status reports whether it did (written = 1). */
+ * solve's displacement change / max |u_prev|, nodes x 3; the change is K^-1 of the input's
+ * residual) into these FP32 device buffers, if it has a previous iteration;
+ * tog_record_status reports whether it did (written = 1). */
 int tog_record_next_step(tog_handle* h, float* input_dev, float* target_dev);
 int tog_record_status(tog_handle* h, int32_t* written);
 

@@ -1,0 +1,33 @@
+"""Learned warm start end to end on a small grid: training data recorded by the
+solver on the device, the network trained by the library's kernels, and the
+same trajectory solved with cold, previous-step, extrapolated and learned
+starts.  Every mode finishes to the same tolerance, so the designs agree; the
+test reports the PCG iterations each start needs (its gain over the
+previous-step start, which measured negative: a start that is closer in the
+energy norm does not shorten Jacobi PCG, whose iteration count is set by the
+conditioning and the tolerance).  The Galerkin step keeps the learned start's
+energy-norm error at or below the previous displacement's."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_learned_warm_start_gain(tg):
+    from topopt_gb300 import learned as LW
+    nels = (32, 16, 16)
+    runs = LW.sample_runs(3, nels, seed=5)
+    X, Y = LW.generate(nels, runs, steps=10)
+    assert X.shape[0] == 3 * 9
+    net = tg.WarmStartNet(tuple(n + 1 for n in nels), batch=1, seed=0)
+    hist = LW.train(net, X, Y, epochs=40, lr=1e-3)
+    assert hist[-1] < 0.5 * hist[0]
+    ev = LW.evaluate(nels, runs[0], 10, net)
+    c = {m: r["compliance"][-1] for m, r in ev.items()}
+    for m in c:   # same tolerance, same trajectory
+        assert abs(c[m] - c["previous"]) <= 1e-6 * abs(c["previous"]), (m, c)
+    its = {m: r["cg_iters_mean"] for m, r in ev.items()}
+    print("mean PCG iterations per design iteration:", its,
+          "learned / previous = %.3f" % (its["learned"] / its["previous"]))
+    assert all(np.isfinite(v) and v > 0 for v in its.values())
+    net.close()

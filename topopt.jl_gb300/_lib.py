@@ -94,6 +94,7 @@ SIGNATURES = {
     "tog_nn_gradients": (C.c_int, [_H, C.c_void_p, C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_float)]),
     "tog_nn_train_step": (C.c_int, [_H, C.c_void_p, C.c_void_p, C.c_float, C.POINTER(C.c_double)]),
     "tog_set_warm_start_net": (C.c_int, [_H, _H]),
+    "tog_keep_previous_state": (C.c_int, [_H]),
     "tog_record_next_step": (C.c_int, [_H, C.c_void_p, C.c_void_p]),
     "tog_record_status": (C.c_int, [_H, _I32]),
     "tog_oc_update_noalloc": (C.c_int, [C.c_int64, _D, _D, _D, _D, C.c_double, C.c_double, _D, _D, C.c_void_p]),

@@ -119,10 +119,12 @@ struct tog_handle {
     // learned warm start (3D): network, previous-iteration state and recording hook
     tog_nn* net = nullptr;
     double* d_vars_prev = nullptr;   // physical densities of the previous design iteration
-    double* d_uprev = nullptr;       // displacement before the solve (recording)
+    double* d_uprev = nullptr;       // displacement before the solve
+    double* d_du_last = nullptr;     // displacement change of the previous design iteration
+    bool have_du = false;
     float* d_nn_in = nullptr;        // network input (nodes x 8)
     float* d_nn_out = nullptr;       // network output (nodes x 3)
-    double* d_nn_sc = nullptr;       // max |u|, max |f|, step length alpha
+    double* d_nn_sc = nullptr;       // max |u|, max |f|, step lengths along the two directions
     double* d_nn_part = nullptr;
     unsigned* d_nn_cnt = nullptr;
     bool have_prev = false;
@@ -576,7 +578,7 @@ int solve_fp32_ir(tog_handle* h, double rtol, double abstol, int maxit, int warm
 // ---------------------------------------------------------------------------
 constexpr int kNnBlocks = 1024;   // grid of the warm-start reductions (partials sized for it)
 
-// sc[0] = max |u| (1 when zero), sc[1] = max |f| (1 when zero)
+// sc[0] = max |u| (1 when zero), sc[1] = max |r0| (1 when zero)
 __global__ void k_nn_scales(const double* __restrict__ u, const double* __restrict__ f, long long n,
                             double* partials, unsigned* cnt, double* sc) {
     double v[2] = {0.0, 0.0};
@@ -592,7 +594,9 @@ __global__ void k_nn_scales(const double* __restrict__ u, const double* __restri
 }
 
 // network input per node: mean of the adjacent cells' new physical density and of
-// its change, u / max|u| and f / max|f| (internal AoS dof layout 3 n + c)
+// its change, u / max|u| and the residual r0 = f - K(rho_new) u over max|r0|
+// (internal AoS dof layout 3 n + c).  The target, the solve's correction, is
+// K^-1 r0: the network learns an approximate inverse of K(rho) applied to r0.
 __global__ void k_nn_input(Dims D, const double* __restrict__ vars, const double* __restrict__ prev,
                            const double* __restrict__ u, const double* __restrict__ f, const double* __restrict__ sc,
                            float* __restrict__ out) {
@@ -622,35 +626,66 @@ __global__ void k_nn_input(Dims D, const double* __restrict__ vars, const double
     }
 }
 
-// correction direction d = max|u| * network output, zero at fixed dofs
+// correction direction d = network output (trained on the density-weighted
+// correction rho~ (u_new - u_prev): in near-void regions the displacement is barely
+// constrained and a guess there only adds work for PCG), zero at fixed dofs
 __global__ void k_nn_direction(const float* __restrict__ y, const uint8_t* __restrict__ fixmask,
-                               const double* __restrict__ sc, double* __restrict__ d, long long nnodes) {
+                               double* __restrict__ d, long long nnodes) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < 3 * nnodes;
          i += (long long)gridDim.x * blockDim.x) {
         const long long n = i / 3;
         const int c = (int)(i - 3 * n);
-        d[i] = ((fixmask[n] >> c) & 1u) ? 0.0 : sc[0] * (double)y[i];
+        d[i] = ((fixmask[n] >> c) & 1u) ? 0.0 : (double)y[i];
     }
 }
 
-// Galerkin step length along d: alpha = d.r0 / d.Kd (0 unless d.Kd > 0), sc[2]
-__global__ void k_nn_alpha(const double* __restrict__ d, const double* __restrict__ r0, const double* __restrict__ kd,
-                           long long n, double* partials, unsigned* cnt, double* sc) {
-    double v[2] = {0.0, 0.0};
+// Galerkin step on span{d1, d2} (d2 may be absent): minimise the energy norm of the
+// error, i.e. solve [d1.Kd1 d1.Kd2; d2.Kd1 d2.Kd2] c = [d1.r0; d2.r0] with r0 = f - K u.
+// A singular or indefinite 2 x 2 system falls back to the better single direction;
+// a direction with d.Kd <= 0 gets no step.  c -> sc[2], sc[3].
+__global__ void k_nn_galerkin(const double* __restrict__ d1, const double* __restrict__ kd1,
+                              const double* __restrict__ d2, const double* __restrict__ kd2,
+                              const double* __restrict__ r0, long long n, double* partials, unsigned* cnt,
+                              double* sc) {
+    double v[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        v[0] = fma(d[i], r0[i], v[0]);
-        v[1] = fma(d[i], kd[i], v[1]);
+        const double a = d1 ? d1[i] : 0.0, b = d2 ? d2[i] : 0.0;
+        v[0] = fma(a, kd1 ? kd1[i] : 0.0, v[0]);   // d1.Kd1
+        v[1] = fma(a, kd2 ? kd2[i] : 0.0, v[1]);   // d1.Kd2
+        v[2] = fma(b, kd2 ? kd2[i] : 0.0, v[2]);   // d2.Kd2
+        v[3] = fma(a, r0[i], v[3]);                 // d1.r0
+        v[4] = fma(b, r0[i], v[4]);                 // d2.r0
     }
-    double tot[2];
-    if (grid_reduce_last<2>(v, partials, cnt, tot) && threadIdx.x == 0)
-        sc[2] = (tot[1] > 0.0 && isfinite(tot[0] / tot[1])) ? tot[0] / tot[1] : 0.0;
+    double t[5];
+    if (grid_reduce_last<5>(v, partials, cnt, t) && threadIdx.x == 0) {
+        const double a11 = t[0], a12 = t[1], a22 = t[2], b1 = t[3], b2 = t[4];
+        double c1 = a11 > 0.0 ? b1 / a11 : 0.0, c2 = a22 > 0.0 ? b2 / a22 : 0.0;
+        // energy decrease of each single direction: b^2 / a
+        const double g1 = a11 > 0.0 ? b1 * c1 : 0.0, g2 = a22 > 0.0 ? b2 * c2 : 0.0;
+        const double det = a11 * a22 - a12 * a12;
+        if (a11 > 0.0 && a22 > 0.0 && det > 1e-10 * a11 * a22) {
+            c1 = (b1 * a22 - b2 * a12) / det;
+            c2 = (b2 * a11 - b1 * a12) / det;
+        } else if (g1 >= g2) {
+            c2 = 0.0;
+        } else {
+            c1 = 0.0;
+        }
+        sc[2] = isfinite(c1) ? c1 : 0.0;
+        sc[3] = isfinite(c2) ? c2 : 0.0;
+    }
 }
 
-__global__ void k_nn_step(double* __restrict__ u, const double* __restrict__ d, const double* __restrict__ sc,
-                          long long n) {
-    const double a = sc[2];
+__global__ void k_nn_step(double* __restrict__ u, const double* __restrict__ d1, const double* __restrict__ d2,
+                          const double* __restrict__ sc, long long n) {
+    const double c1 = sc[2], c2 = sc[3];
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        u[i] = fma(a, d[i], u[i]);
+        u[i] = fma(c1, d1 ? d1[i] : 0.0, fma(c2, d2 ? d2[i] : 0.0, u[i]));
+}
+
+__global__ void k_sub(const double* __restrict__ a, const double* __restrict__ b, double* __restrict__ c, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        c[i] = a[i] - b[i];
 }
 
 // training target: (u_new - u_prev) / max|u_prev|
@@ -669,41 +704,55 @@ int nn_buffers(tog_handle* h) {
     };
     A(dalloc(&h->d_vars_prev, h->ncells));
     A(dalloc(&h->d_uprev, h->ndofs));
+    A(dalloc(&h->d_du_last, h->ndofs));
     A(dalloc(&h->d_nn_in, 8 * h->nnodes));
     A(dalloc(&h->d_nn_out, 3 * h->nnodes));
     A(dalloc(&h->d_nn_sc, 4));
-    A(dalloc(&h->d_nn_part, 2 * kNnBlocks));
+    A(dalloc(&h->d_nn_part, 5 * kNnBlocks));
     A(dalloc(&h->d_nn_cnt, 4));
     if (rc != TOG_OK) return rc;
     TOG_CUDA(cudaMemsetAsync(h->d_nn_cnt, 0, 4 * sizeof(unsigned), h->stream));
     h->have_prev = false;
+    h->have_du = false;
     return TOG_OK;
 }
 
 // Before the solve of a design iteration (new physical densities in d_vars, the
-// previous solution in d_u): write the network input (into the recording buffer
-// when one is set) and, with a network attached and apply set, move d_u along the
-// network's correction by the Galerkin step, which never increases the energy
-// norm of the error.
-int nn_before_solve(tog_handle* h, bool apply) {
+// previous solution in d_u): keep u_prev, write the network input (into the
+// recording buffer when one is set) and, for the learned and extrapolated starts,
+// move d_u by the Galerkin step on span{network correction, last change}
+// (learned) or along the last change alone (extrapolated).  Either never increases
+// the energy norm of the error.
+int nn_before_solve(tog_handle* h, bool use_net, bool use_du) {
     cudaStream_t s = h->stream;
     const int nb = (int)std::min<long long>(kNnBlocks, h->ew_blocks(h->ndofs));
-    k_nn_scales<<<nb, kEwThreads, 0, s>>>(h->d_u, h->d_f, h->ndofs, h->d_nn_part, h->d_nn_cnt, h->d_nn_sc);
-    float* in = h->rec_in ? h->rec_in : h->d_nn_in;
-    k_nn_input<<<h->ew_blocks(h->nnodes), kEwThreads, 0, s>>>(h->dims(), h->d_vars, h->d_vars_prev, h->d_u, h->d_f,
-                                                             h->d_nn_sc, in);
-    if (h->rec_in)
-        TOG_CUDA(cudaMemcpyAsync(h->d_uprev, h->d_u, h->ndofs * sizeof(double), cudaMemcpyDeviceToDevice, s));
-    if (apply) {
-        TOG_TRY(refresh_scales(h));
-        TOG_TRY(nn_forward_dev(h->net, in, h->d_nn_out, s));
-        k_nn_direction<<<h->ew_blocks(h->ndofs), kEwThreads, 0, s>>>(h->d_nn_out, h->d_fixmask, h->d_nn_sc, h->d_tmp,
-                                                                   h->nnodes);
-        launch_matvec<double, MV_RESID>(h, s, h->d_u, h->d_r64, h->d_f);       // r0 = f - K u
-        launch_matvec<double, MV_PLAIN>(h, s, h->d_tmp, h->d_q64, nullptr);    // K d
-        k_nn_alpha<<<nb, kEwThreads, 0, s>>>(h->d_tmp, h->d_r64, h->d_q64, h->ndofs, h->d_nn_part, h->d_nn_cnt + 1,
-                                             h->d_nn_sc);
-        k_nn_step<<<h->ew_blocks(h->ndofs), kEwThreads, 0, s>>>(h->d_u, h->d_tmp, h->d_nn_sc, h->ndofs);
+    TOG_CUDA(cudaMemcpyAsync(h->d_uprev, h->d_u, h->ndofs * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    use_du = use_du && h->have_du;
+    const bool input = use_net || h->rec_in;
+    if (!(input || use_du)) return TOG_OK;
+    TOG_TRY(refresh_scales(h));
+    launch_matvec<double, MV_RESID>(h, s, h->d_u, h->d_r64, h->d_f);   // r0 = f - K(rho_new) u
+    float* in = nullptr;
+    if (input) {
+        k_nn_scales<<<nb, kEwThreads, 0, s>>>(h->d_u, h->d_r64, h->ndofs, h->d_nn_part, h->d_nn_cnt, h->d_nn_sc);
+        in = h->rec_in ? h->rec_in : h->d_nn_in;
+        k_nn_input<<<h->ew_blocks(h->nnodes), kEwThreads, 0, s>>>(h->dims(), h->d_vars, h->d_vars_prev, h->d_u,
+                                                                 h->d_r64, h->d_nn_sc, in);
+    }
+    if (use_net || use_du) {
+        double* d1 = nullptr;
+        double* d2 = use_du ? h->d_du_last : nullptr;
+        if (use_net) {
+            TOG_TRY(nn_forward_dev(h->net, in, h->d_nn_out, s));
+            k_nn_direction<<<h->ew_blocks(h->ndofs), kEwThreads, 0, s>>>(h->d_nn_out, h->d_fixmask, h->d_tmp,
+                                                                       h->nnodes);
+            d1 = h->d_tmp;
+            launch_matvec<double, MV_PLAIN>(h, s, d1, h->d_q64, nullptr);          // K d1
+        }
+        if (d2) launch_matvec<double, MV_PLAIN>(h, s, d2, h->d_p64[1], nullptr);   // K d2
+        k_nn_galerkin<<<nb, kEwThreads, 0, s>>>(d1, d1 ? h->d_q64 : nullptr, d2, d2 ? h->d_p64[1] : nullptr, h->d_r64,
+                                                h->ndofs, h->d_nn_part, h->d_nn_cnt + 1, h->d_nn_sc);
+        k_nn_step<<<h->ew_blocks(h->ndofs), kEwThreads, 0, s>>>(h->d_u, d1, d2, h->d_nn_sc, h->ndofs);
     }
     TOG_CUDA(cudaGetLastError());
     return TOG_OK;
@@ -1077,7 +1126,7 @@ int tog_destroy(tog_handle* h) {
     void* ptrs[] = {h->d_int2ref, h->d_ref2int, h->d_fixmask, h->d_vecpool, h->d_vars,    h->d_e64,
                     h->d_e32,     h->d_dinv64,  h->d_dinv32,  h->d_nodal,   h->d_st64,    h->d_st32,
                     h->d_oc,      h->d_partials, h->d_cnt,    h->d_scalar,  h->d_invW,    h->d_soff,
-                    h->d_sw,      h->d_vars_prev, h->d_uprev, h->d_nn_in, h->d_nn_out, h->d_nn_sc,
+                    h->d_sw,      h->d_vars_prev, h->d_uprev, h->d_du_last, h->d_nn_in, h->d_nn_out, h->d_nn_sc,
                     h->d_nn_part, h->d_nn_cnt};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -1307,9 +1356,11 @@ int tog_simp_step(tog_handle* h, int32_t precision, double rtol, int32_t maxiter
     // learned warm start / recording: need the previous iteration's densities and solution
     const bool prev_ok = h->d_vars_prev && h->have_prev && h->u_valid && h->dim == 3;
     const bool learned = warm_start == TOG_WARM_LEARNED && h->net && prev_ok;
+    const bool extrap = (warm_start == TOG_WARM_LEARNED || warm_start == TOG_WARM_EXTRAPOLATE) && prev_ok;
     const bool record = h->rec_in && prev_ok;
     if (!record) h->rec_in = nullptr;
-    if (learned || record) TOG_TRY(nn_before_solve(h, learned));
+    const bool keep = prev_ok;   // u_prev is kept for the next iteration's last change
+    if (learned || extrap || record || keep) TOG_TRY(nn_before_solve(h, learned, extrap));
     tog_solve_stats ss{};
     int rc = do_solve(h, precision, rtol, 0.0, maxiter, warm_start != 0, &ss);
     if (rc != TOG_OK && rc != TOG_NOT_CONVERGED) return rc;
@@ -1317,6 +1368,10 @@ int tog_simp_step(tog_handle* h, int32_t precision, double rtol, int32_t maxiter
         k_nn_target<<<h->ew_blocks(h->ndofs), kEwThreads, 0, h->stream>>>(h->d_u, h->d_uprev, h->d_nn_sc, h->rec_tgt,
                                                                          h->ndofs);
         h->rec_written = 1;
+    }
+    if (keep) {   // last change, for the next iteration's extrapolated / learned start
+        k_sub<<<h->ew_blocks(h->ndofs), kEwThreads, 0, h->stream>>>(h->d_u, h->d_uprev, h->d_du_last, h->ndofs);
+        h->have_du = true;
     }
     h->rec_in = nullptr;
     h->rec_tgt = nullptr;
@@ -1361,6 +1416,12 @@ int tog_set_warm_start_net(tog_handle* h, tog_nn* nn) {
     }
     h->net = nn;
     return TOG_OK;
+}
+
+int tog_keep_previous_state(tog_handle* h) {
+    TOG_TRY(check_handle(h));
+    if (h->dim != 3) return fail(TOG_ERR_ARG, "previous-state starts are for 3D grids");
+    return nn_buffers(h);
 }
 
 int tog_record_next_step(tog_handle* h, float* input_dev, float* target_dev) {

@@ -1,8 +1,8 @@
 // Learned warm start: a small 3D convolutional encoder-decoder that maps the
 // state of a SIMP design iteration on a structured hex8 grid (per node: the
 // new filtered density, its change since the previous iteration, the previous
-// displacement and the load, both scaled) to a correction of the previous
-// displacement.  It has no counterpart in TopOpt.jl.
+// displacement and its residual under the new densities, both scaled) to a
+// correction of the previous displacement.  It has no counterpart in TopOpt.jl.
 //
 // Architecture (channels-last BF16 activations, every channel count padded to
 // a multiple of 16, 3x3x3 kernels, zero padding 1):

@@ -2,8 +2,9 @@
 
 The network (WarmStartNet, tensor-core kernels of libtopopt_gb300) maps the
 state of a design iteration (new filtered densities and their change, the
-previous displacement, the load) to a correction d of the previous
-displacement.  The solver moves u_prev along d by the Galerkin step
+previous displacement and its residual r0 = f - K(new densities) u_prev) to a
+correction d of the previous displacement; the exact correction is K^-1 r0, so
+the network learns an approximate inverse of K(rho) applied to the residual.  The solver moves u_prev along d by the Galerkin step
 alpha = d.r0 / d.K d before its PCG solve, so a poor prediction can never make
 the start worse in the energy norm, and every solve still finishes to the same
 residual tolerance: plain PCG stays both the fallback and the judge.
@@ -50,11 +51,17 @@ def generate(nels, runs, steps, rmin=1.5, rtol=1e-8, device="cuda"):
     k = 0
     for run in runs:
         s, loop = make_loop(nels, run, rmin, rtol, True)
+        s.enable_previous_state()   # from the first iteration on, so the second one records
         for it in range(steps):
             if it > 0:
                 s.record_next_step(X[k:k + 1], Y[k:k + 1])
             loop.step()
             if it > 0 and s.record_status():
+                # target: the density-weighted correction rho~ (u_new - u_prev) (near-void
+                # displacements are barely constrained and unpredictable), of unit RMS:
+                # only its direction matters, the solver rescales it by the Galerkin step
+                Y[k].mul_(X[k, ..., 0:1])
+                Y[k].div_(Y[k].pow(2).mean().sqrt().clamp_min(1e-30))
                 k += 1
         s.close()
     torch.cuda.synchronize()
@@ -78,7 +85,7 @@ def train(net, X, Y, epochs, lr=1e-3, seed=0, lr_min=1e-4):
     return hist
 
 
-def evaluate(nels, run, steps, net=None, rmin=1.5, rtol=1e-8, modes=("cold", "previous", "learned")):
+def evaluate(nels, run, steps, net=None, rmin=1.5, rtol=1e-8, modes=("cold", "previous", "extrapolate", "learned")):
     """Run the same seeded SIMP trajectory once per warm-start mode and report, per
     mode, the inner PCG iterations of every design iteration and the wall time per
     design iteration (the first iteration excluded: it has no previous state)."""
@@ -88,6 +95,8 @@ def evaluate(nels, run, steps, net=None, rmin=1.5, rtol=1e-8, modes=("cold", "pr
         s, loop = make_loop(nels, run, rmin, rtol, mode)
         if mode == "learned":
             s.attach_network(net)
+        elif mode == "extrapolate":
+            s.enable_previous_state()
         its, comp, t = [], [], []
         for _ in range(steps):
             torch.cuda.synchronize()
@@ -115,8 +124,8 @@ def main(argv=None):
     ap.add_argument("--nels", default="96,48,48")
     ap.add_argument("--runs", type=int, default=40)
     ap.add_argument("--steps", type=int, default=26)
-    ap.add_argument("--epochs", type=int, default=8)
-    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--epochs", type=int, default=24)
+    ap.add_argument("--lr", type=float, default=3e-4)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--eval-runs", type=int, default=2)
     ap.add_argument("--eval-steps", type=int, default=20)
@@ -133,11 +142,15 @@ def main(argv=None):
     torch.cuda.synchronize()
     t_train = time.time() - t0
     np.save(a.out, net.get_params())
+    Xv, Yv = generate(nels, sample_runs(a.eval_runs, nels, a.seed + 1000), a.steps)
+    val = float(np.mean([net.gradients(Xv[i:i + 1], Yv[i:i + 1])[0] for i in range(Xv.shape[0])]))
+    del Xv, Yv
     evals = [evaluate(nels, r, a.eval_steps, net) for r in sample_runs(a.eval_runs, nels, a.seed + 1000)]
     log = {"nels": nels, "runs": a.runs, "steps": a.steps, "samples": int(X.shape[0]), "epochs": a.epochs,
            "lr": a.lr, "seed": a.seed, "generate_s": t_gen, "train_s": t_train,
            "train_ms_per_step": 1e3 * t_train / (a.epochs * X.shape[0]), "loss_per_epoch": hist,
-           "target_mean_square": float(Y.pow(2).mean()), "evaluation": evals}
+           "target_mean_square": float(Y.pow(2).mean()), "validation_loss_heldout_runs": val,
+           "evaluation": evals}
     with open(a.out.rsplit(".", 1)[0] + ".json", "w") as f:
         json.dump(log, f, indent=1)
     print(json.dumps({k: v for k, v in log.items() if k != "evaluation"}))

@@ -156,7 +156,7 @@ class GB300Solver:
 
 
 PRECISIONS = {"fp64": L.TOG_FP64, "fp32_ir": L.TOG_FP32_IR}
-WARM_MODES = {False: 0, True: 1, 0: 0, 1: 1, 2: 2, "cold": 0, "previous": 1, "learned": 2}
+WARM_MODES = {False: 0, True: 1, 0: 0, 1: 1, 2: 2, 3: 3, "cold": 0, "previous": 1, "learned": 2, "extrapolate": 3}
 
 
 class GB300FEASolver:
@@ -175,8 +175,9 @@ class GB300FEASolver:
         if precision not in PRECISIONS:
             raise ValueError("precision must be one of %s" % sorted(PRECISIONS))
         self.precision = precision
-        # False / True (previous displacement) / "learned" (previous displacement moved
-        # along an attached WarmStartNet's correction; SIMP steps of 3D problems)
+        # False / True (previous displacement) / "learned" (previous displacement moved by
+        # the Galerkin step on an attached WarmStartNet's correction and the last change) /
+        # "extrapolate" (the same step along the last change alone); SIMP steps of 3D problems
         self.warm_start = WARM_MODES[warm_start]
         self.net = None
         d = L.ProblemDesc()
@@ -212,6 +213,10 @@ class GB300FEASolver:
         """Use a WarmStartNet (created for this grid's nodes, batch 1) for warm_start="learned"."""
         L.check(L.lib().tog_set_warm_start_net(self.handle, net.handle if net is not None else None))
         self.net = net
+
+    def enable_previous_state(self):
+        """Keep the previous iteration's state on the device (needed by warm_start="extrapolate")."""
+        L.check(L.lib().tog_keep_previous_state(self.handle))
 
     def record_next_step(self, inp, target):
         """The next SIMP step writes its network input / target into these CUDA tensors
