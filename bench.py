@@ -49,7 +49,7 @@ def read_peaks():
 def read_traffic(ncells):
     """DRAM bytes per launch of the PCG operator kernel: the committed ncu summary's
     bytes per cell (captured on a case larger than L2) scaled by the cell count."""
-    p = os.path.join(ROOT, "profiles", "k_matvec3_fp32_pcg_256x128x128.md")
+    p = os.path.join(ROOT, "profiles", "k_mv3_fp32_pcg_256x128x128.md")
     try:
         for line in open(p):
             if line.startswith("traffic_bytes_per_element:"):
