@@ -152,9 +152,10 @@ struct tog_handle {
         D.ncells = ncells;
         return D;
     }
+    int upd_per_sm = 2;        // PCG update blocks per SM (TOG_UPD_BLOCKS_PER_SM; 2 measured fastest)
     int upd_blocks() const {   // PCG update grid: a few blocks per SM, grid-stride over dof groups
         long long b = (3 * nnodes + 4LL * kEwThreads - 1) / (4LL * kEwThreads);
-        const long long cap = (long long)nsm * 4;   // few blocks: the last-block reduction tail grows with the grid
+        const long long cap = (long long)nsm * upd_per_sm;   // the last-block reduction tail grows with the grid
         return (int)std::max(1LL, std::min(b, cap));
     }
     int ew_blocks(long long n) const {
@@ -983,6 +984,7 @@ int tog_create(const tog_problem_desc* desc, tog_handle** out) {
     }
     h->stream = h->own;
     if (const char* e = std::getenv("TOG_RU_DELTA")) h->ru_delta = std::min(0.9, std::max(1e-6, std::atof(e)));
+    if (const char* e = std::getenv("TOG_UPD_BLOCKS_PER_SM")) h->upd_per_sm = std::min(32, std::max(1, std::atoi(e)));
     if (dim == 3) {
         // z-chunk length: minimise (rounds of resident blocks) x (layers + prologue)
         h->nt[0] = (h->nel[0] + 31) / 32;

@@ -553,18 +553,14 @@ __global__ void __launch_bounds__(256) k_pcg_update3(const Mv3Args<T> A, T* __re
         const float4* __restrict__ p4 = reinterpret_cast<const float4*>(p);
         float4* __restrict__ x4 = reinterpret_cast<float4*>(x);
         float4* __restrict__ r4 = reinterpret_cast<float4*>(r);
-        for (unsigned g = blockIdx.x * blockDim.x + threadIdx.x; g < nv; g += gridDim.x * blockDim.x) {
-            const float4 qv = q4[g], pv = p4[g], xv = x4[g], rv = r4[g];
+        // two float4 groups per thread and round, every load issued before the first store
+        const unsigned stride = gridDim.x * blockDim.x;
+        auto group = [&](unsigned g, const float4& qv, const float4& pv, const float4& xv, const float4& rv,
+                         unsigned m0, unsigned m1, float d0, float d1, unsigned c0) {
             const float qa[4] = {qv.x, qv.y, qv.z, qv.w};
             const float pa[4] = {pv.x, pv.y, pv.z, pv.w};
             const float xa[4] = {xv.x, xv.y, xv.z, xv.w}, ra[4] = {rv.x, rv.y, rv.z, rv.w};
             float xo[4], ro[4];
-            const unsigned f0 = 4u * g;
-            const unsigned n0 = f0 / 3u;
-            const unsigned c0 = f0 - 3u * n0;
-            const unsigned nb = n0 + 1 < nnodes ? n0 + 1 : n0;
-            const unsigned m0 = A.fixmask[n0], m1 = A.fixmask[nb];
-            const float d0 = (float)A.dinv[n0], d1 = (float)A.dinv[nb];
 #pragma unroll
             for (int t = 0; t < 4; ++t) {
                 const unsigned c = c0 + t;              // 0..5: node n0 (c < 3) or n0 + 1
@@ -582,6 +578,32 @@ __global__ void __launch_bounds__(256) k_pcg_update3(const Mv3Args<T> A, T* __re
             }
             x4[g] = make_float4(xo[0], xo[1], xo[2], xo[3]);
             r4[g] = make_float4(ro[0], ro[1], ro[2], ro[3]);
+        };
+        auto node_of = [&](unsigned g, unsigned& n0, unsigned& nb, unsigned& c0) {
+            const unsigned f0 = 4u * g;
+            n0 = f0 / 3u;
+            c0 = f0 - 3u * n0;
+            nb = n0 + 1 < nnodes ? n0 + 1 : n0;
+        };
+        unsigned g = blockIdx.x * blockDim.x + threadIdx.x;
+        for (; g + stride < nv; g += 2 * stride) {
+            const unsigned h2 = g + stride;
+            unsigned na, nab, ca, nc, ncb, cc2;
+            node_of(g, na, nab, ca);
+            node_of(h2, nc, ncb, cc2);
+            const float4 qa = q4[g], pa = p4[g], xa = x4[g], ra = r4[g];
+            const float4 qb = q4[h2], pb = p4[h2], xb = x4[h2], rb = r4[h2];
+            const unsigned ma0 = A.fixmask[na], ma1 = A.fixmask[nab], mb0 = A.fixmask[nc], mb1 = A.fixmask[ncb];
+            const float da0 = (float)A.dinv[na], da1 = (float)A.dinv[nab], db0 = (float)A.dinv[nc],
+                        db1 = (float)A.dinv[ncb];
+            group(g, qa, pa, xa, ra, ma0, ma1, da0, da1, ca);
+            group(h2, qb, pb, xb, rb, mb0, mb1, db0, db1, cc2);
+        }
+        if (g < nv) {
+            unsigned na, nab, ca;
+            node_of(g, na, nab, ca);
+            group(g, q4[g], p4[g], x4[g], r4[g], A.fixmask[na], A.fixmask[nab], (float)A.dinv[na],
+                  (float)A.dinv[nab], ca);
         }
         // tail dofs
         for (unsigned f = 4u * nv + blockIdx.x * blockDim.x + threadIdx.x; f < ndofs; f += gridDim.x * blockDim.x) {
