@@ -105,14 +105,22 @@ def dist_setup():
     return ws, rank, local
 
 
-def max_over_ranks(v, ws):
+def max_over_ranks(v, ws, device="cuda"):
+    """The slowest rank's time (every rank gets it): NCCL on the GPU ranks of the bench,
+    gloo on CPU in the tests."""
     if ws == 1:
         return v
     import torch
     import torch.distributed as dist
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    t = torch.tensor([v], dtype=torch.float64, device=device)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_rate(units_per_rank, ws, t_max):
+    """Whole-job throughput of N independent replicas: all ranks' units over the slowest
+    rank's time (weak scaling, no data-path collective)."""
+    return ws * units_per_rank / t_max
 
 
 def barrier(ws):
@@ -329,7 +337,7 @@ def run_ours(args):
     launches = L.lib().tog_launch_count() - l0
     t_dev = e0.elapsed_time(e1) / 1e3
     t_dev = max_over_ranks(t_dev, ws)
-    value = ws * args.steps / t_dev
+    value = replica_rate(args.steps, ws, t_dev)
     clocks = clk.summary()
 
     if args.no_extra:
