@@ -17,6 +17,7 @@
 #include "tog_kernels.cuh"
 #include "tog_mv3.cuh"
 #include "tog_mv3x2.cuh"
+#include "tog_march3.cuh"
 
 using namespace tog;
 
@@ -133,7 +134,9 @@ struct tog_handle {
     // 3D operator tiling: tiles of 32 x MV3_BY elements, LZ layers per z chunk
     int nt[3] = {1, 1, 1};
     int LZ = 8;
-    bool mv3_scalar = true;    // FP32 operator: k_mv3 (scalar) unless TOG_MV3_KERNEL=pair
+    bool mv3_scalar = true;    // FP32 tile operator: k_mv3 (scalar) unless TOG_MV3_KERNEL=pair
+    bool mv3_march = true;     // FP32 PCG operator: k_march3 unless TOG_MV3_KERNEL=tile / pair
+    int march_grid = 0;        // persistent grid of k_march3
     double ru_delta = 0.1;     // FP32-IR reliable-update trigger: residual reduction factor (TOG_RU_DELTA)
     float* d_side32[8] = {};
     double* d_side64[8] = {};
@@ -316,7 +319,10 @@ void launch_matvec(tog_handle* h, cudaStream_t s, const T* x, T* y, const double
         Mv3Args<T> A = mv3_args<T>(h);
         A.x = x;
         if (MODE == MV_RESID) A.st = h->d_st64;
-        if (std::is_same<T, float>::value && MODE != MV_RESID && !h->mv3_scalar)
+        if (std::is_same<T, float>::value && MODE == MV_PCG && h->mv3_march)
+            k_march3<<<h->march_grid, 32 * kM3Warps, 0, s>>>(*reinterpret_cast<const Mv3Args<float>*>(&A),
+                                                            (h->nn[0] + 29) / 30);
+        else if (std::is_same<T, float>::value && MODE != MV_RESID && !h->mv3_scalar)
             launch_mv3x2<MODE == MV_RESID ? MV_PLAIN : MODE>(h, s, *reinterpret_cast<const Mv3Args<float>*>(&A));
         else
             launch_mv3<T, MODE>(h, s, A);
@@ -346,7 +352,9 @@ void launch_pcg_update(tog_handle* h, cudaStream_t s) {
         const long long n_side = (long long)(h->nt[0] - 1) * h->nn[1] * h->nn[2] +
                                  (long long)(h->nt[1] - 1) * h->nn[0] * h->nn[2] +
                                  (long long)(h->nt[2] - 1) * h->nn[0] * h->nn[1];
-        if (n_side > 0) {
+        // the FP32 march writes complete q: no tile-boundary partials to gather
+        const bool march = std::is_same<T, float>::value && h->mv3_march;
+        if (n_side > 0 && !march) {
             const long long nbs = std::min<long long>((n_side + kEwThreads - 1) / kEwThreads, (long long)h->nsm * 8);
             k_side_gather3<T><<<(int)nbs, kEwThreads, 0, s>>>(A);
             TOG_LAUNCHED(1);
@@ -990,7 +998,14 @@ int tog_create(const tog_problem_desc* desc, tog_handle** out) {
         h->nt[0] = (h->nel[0] + 31) / 32;
         h->nt[1] = (h->nel[1] + MV3_BY - 1) / MV3_BY;
         const long long txy = (long long)h->nt[0] * h->nt[1];
-        if (const char* e = std::getenv("TOG_MV3_KERNEL")) h->mv3_scalar = std::string(e) != "pair";
+        if (const char* e = std::getenv("TOG_MV3_KERNEL")) {
+            h->mv3_scalar = std::string(e) != "pair";
+            h->mv3_march = std::string(e) == "march";
+        }
+        int bps = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_march3, 32 * kM3Warps, 0) != cudaSuccess || bps < 1)
+            bps = 1;
+        h->march_grid = h->nsm * bps;
         int occ = 0;
         cudaError_t oe;
         if (h->mv3_scalar) {
@@ -1026,6 +1041,7 @@ int tog_create(const tog_problem_desc* desc, tog_handle** out) {
     maxb = std::max(maxb, (size_t)((h->nnodes + kEwThreads - 1) / kEwThreads));
     maxb = std::max(maxb, (size_t)g2.x * g2.y);
     maxb = std::max(maxb, (size_t)h->nsm * 8);
+    maxb = std::max(maxb, (size_t)h->march_grid);
     h->npartials = maxb * 4;
     int rc = TOG_OK;
     auto A = [&](int r) {
