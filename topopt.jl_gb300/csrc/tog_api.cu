@@ -137,6 +137,7 @@ struct tog_handle {
     bool mv3_scalar = true;    // FP32 tile operator: k_mv3 (scalar) unless TOG_MV3_KERNEL=pair
     bool mv3_march = true;     // FP32 PCG operator: k_march3 unless TOG_MV3_KERNEL=tile / pair
     int march_grid = 0;        // persistent grid of k_march3
+    int march_nband = 1, march_lzb = 1;   // its z bands per node column and their height
     double ru_delta = 0.1;     // FP32-IR reliable-update trigger: residual reduction factor (TOG_RU_DELTA)
     float* d_side32[8] = {};
     double* d_side64[8] = {};
@@ -321,7 +322,7 @@ void launch_matvec(tog_handle* h, cudaStream_t s, const T* x, T* y, const double
         if (MODE == MV_RESID) A.st = h->d_st64;
         if (std::is_same<T, float>::value && MODE == MV_PCG && h->mv3_march)
             k_march3<<<h->march_grid, 32 * kM3Warps, 0, s>>>(*reinterpret_cast<const Mv3Args<float>*>(&A),
-                                                            (h->nn[0] + 29) / 30);
+                                                            (h->nn[0] + 29) / 30, h->march_nband, h->march_lzb);
         else if (std::is_same<T, float>::value && MODE != MV_RESID && !h->mv3_scalar)
             launch_mv3x2<MODE == MV_RESID ? MV_PLAIN : MODE>(h, s, *reinterpret_cast<const Mv3Args<float>*>(&A));
         else
@@ -1006,6 +1007,21 @@ int tog_create(const tog_problem_desc* desc, tog_handle** out) {
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_march3, 32 * kM3Warps, 0) != cudaSuccess || bps < 1)
             bps = 1;
         h->march_grid = h->nsm * bps;
+        {   // z bands: fewest (rounds of the warp grid) x (planes walked per band, halo included)
+            const long long ncol = (long long)((h->nn[0] + 29) / 30) * h->nn[1];
+            const long long gw = (long long)h->march_grid * kM3Warps;
+            long long best = -1;
+            for (int b = 1; b <= h->nn[2]; ++b) {
+                const int lz = (h->nn[2] + b - 1) / b;
+                const long long rounds = (ncol * b + gw - 1) / gw;
+                const long long cost = rounds * (lz + 2);
+                if (best < 0 || cost < best) {
+                    best = cost;
+                    h->march_nband = b;
+                    h->march_lzb = lz;
+                }
+            }
+        }
         int occ = 0;
         cudaError_t oe;
         if (h->mv3_scalar) {
