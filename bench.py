@@ -49,7 +49,7 @@ def read_peaks():
 def read_traffic(ncells):
     """DRAM bytes per launch of the PCG operator kernel: the committed ncu summary's
     bytes per cell (captured on a case larger than L2) scaled by the cell count."""
-    p = os.path.join(ROOT, "profiles", "k_mv3_fp32_pcg_256x128x128.md")
+    p = os.path.join(ROOT, "profiles", "k_march3_fp32_pcg_256x128x128.md")
     try:
         for line in open(p):
             if line.startswith("traffic_bytes_per_element:"):
@@ -404,7 +404,7 @@ def run_ours(args):
                     "%d..%d)" % (args.warmup + 1, args.warmup + k64, args.warmup + 1, args.warmup + args.steps)}
     s64.close()
 
-    # ---- roofline of the dominant kernel (FP32 PCG operator, k_mv3<float, PCG>) and of the
+    # ---- roofline of the dominant kernel (FP32 PCG operator, k_march3) and of the
     #      PCG update, each timed alone with CUDA events on the launching stream
     peaks, src = read_peaks()
 
@@ -425,7 +425,7 @@ def run_ours(args):
     t_k, nbytes = time_kernel(0, 200)
     t_u, ubytes = time_kernel(1, 200)
     achieved = nbytes / t_k / 1e9
-    roof = {"bound": "hbm", "kernel": "k_mv3<float, PCG>", "achieved": achieved, "peak": peaks["hbm_gbs"],
+    roof = {"bound": "hbm", "kernel": "k_march3 (FP32 PCG operator)", "achieved": achieved, "peak": peaks["hbm_gbs"],
             "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "traffic": read_traffic(n),
             "algorithmic_bytes_per_launch": nbytes, "us_per_launch": t_k * 1e6,
             "peak_source": src + " (MEASURED_PEAKS.json hbm_gbs, burst copy)" if src == "measured" else src,

@@ -1542,8 +1542,9 @@ int tog_kernel_bytes(tog_handle* h, int32_t kernel, int32_t precision, double* b
     if (!bytes || kernel < 0 || kernel > 1) return fail(TOG_ERR_ARG, "bad kernel id or null output");
     const double s = precision == TOG_FP64 ? 8.0 : 4.0;
     const double N = (double)h->ndofs, Nn = (double)h->nnodes, E = (double)h->ncells;
-    if (kernel == 0)   // reads r, p_old, D^-1, E_e, mask; writes p, q
-        *bytes = 4.0 * s * N + s * Nn + s * E + Nn;
+    const bool march = h->dim == 3 && precision != TOG_FP64 && h->mv3_march;
+    if (kernel == 0)   // reads r, p_old, D^-1, E_e (and the fixed mask, except the 3D march); writes p, q
+        *bytes = 4.0 * s * N + s * Nn + s * E + (march ? 0.0 : Nn);
     else               // reads q, p, x, r, D^-1, mask; writes x, r
         *bytes = 6.0 * s * N + s * Nn + Nn;
     return TOG_OK;
