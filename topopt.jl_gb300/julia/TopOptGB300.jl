@@ -32,6 +32,7 @@ using ChainRulesCore
 using Ferrite
 
 export GB300Solver, GB300FEASolver, GB300DensityFilter, GB300SensFilter, oc_update!, simp_step!
+export BatchedSIMP, batch_step!, batch_results, WarmStartNet, attach_network!
 
 const libtog = joinpath(@__DIR__, "..", "libtopopt_gb300.so")
 
@@ -259,6 +260,87 @@ function design(s::GB300FEASolver)
     x = zeros(getncells(s.problem))
     check(ccall((:tog_get_design, libtog), Cint, (Ptr{Cvoid}, Ptr{Float64}), s.handle, x))
     return x
+end
+
+# --------------------------------------------------------------------------- batched 2D
+mutable struct BatchStats
+    steps::Int32
+    pcg_loops::Int32
+    failed::Int32
+    reliable_updates::Int32
+end
+BatchStats() = BatchStats(0, 0, 0, 0)
+
+"""
+    BatchedSIMP(nelx, nely, load_j, volfrac, rmin; rtol=1e-8, E=1.0, nu=0.3, xmin=1e-9, p=3.0)
+
+Many independent 2D cantilevers (left edge clamped, unit load [0, -1] at node (nelx, load_j)),
+each design iteration of all of them one CUDA graph launch (no TopOpt.jl counterpart: there a
+user loops over problems).  `autotune!`, `batch_step!`, `batch_results`.
+"""
+mutable struct BatchedSIMP
+    handle::Ptr{Cvoid}
+    n::Int
+end
+function BatchedSIMP(nelx, nely, load_j, volfrac, rmin; rtol=1e-8, E=1.0, nu=0.3, xmin=1e-9, p=3.0)
+    n = length(nelx)
+    desc = ProblemDesc(Int32(2), (Int32(0), Int32(0), Int32(0)), (1.0, 1.0, 1.0), E, nu, Int32(0), xmin, p)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:tog_batch_create, libtog), Cint,
+                (Int32, Ptr{Int32}, Ptr{Int32}, Ptr{Int32}, Ptr{Float64}, Ptr{Float64}, Ref{ProblemDesc}, Float64,
+                 Int32, Ref{Ptr{Cvoid}}),
+                n, Int32.(nelx), Int32.(nely), Int32.(load_j), Float64.(volfrac), Float64.(rmin), desc, rtol, 0, h))
+    b = BatchedSIMP(h[], n)
+    finalizer(b) do x
+        x.handle == C_NULL || ccall((:tog_batch_destroy, libtog), Cint, (Ptr{Cvoid},), x.handle)
+    end
+    return b
+end
+function autotune!(b::BatchedSIMP)
+    rows = Ref{Int32}(0)
+    check(ccall((:tog_batch_autotune, libtog), Cint, (Ptr{Cvoid}, Ref{Int32}), b.handle, rows))
+    return rows[]
+end
+function batch_step!(b::BatchedSIMP)
+    st = Ref(BatchStats())
+    check(ccall((:tog_batch_step, libtog), Cint, (Ptr{Cvoid}, Ref{BatchStats}), b.handle, st))
+    return st[]
+end
+function batch_results(b::BatchedSIMP)
+    c, ch, it = zeros(b.n), zeros(b.n), zeros(Int32, b.n)
+    check(ccall((:tog_batch_results, libtog), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Int32}),
+                b.handle, c, ch, it))
+    return c, ch, it
+end
+
+# --------------------------------------------------------------------------- learned warm start
+"""
+    WarmStartNet(nodes; seed=0, params=nothing)
+
+The learned warm-start network of the library (tensor-core conv3d encoder-decoder) for a 3D
+node grid `nodes = (nnx, nny, nnz)`, optionally loaded with a trained FP32 parameter vector.
+`attach_network!(solver, net)` then makes `simp_step!` start from the Galerkin-corrected
+previous displacement when the solver's `warm_start` is 2 (no TopOpt.jl counterpart).
+"""
+mutable struct WarmStartNet
+    handle::Ptr{Cvoid}
+end
+function WarmStartNet(nodes; seed=0, params=nothing)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:tog_nn_create, libtog), Cint, (Ptr{Int32}, Int32, UInt64, Ref{Ptr{Cvoid}}),
+                Int32.(collect(nodes)), Int32(1), UInt64(seed), h))
+    net = WarmStartNet(h[])
+    finalizer(net) do x
+        x.handle == C_NULL || ccall((:tog_nn_destroy, libtog), Cint, (Ptr{Cvoid},), x.handle)
+    end
+    if params !== nothing
+        check(ccall((:tog_nn_set_params, libtog), Cint, (Ptr{Cvoid}, Ptr{Float32}), net.handle, Float32.(params)))
+    end
+    return net
+end
+function attach_network!(s::GB300FEASolver, net::WarmStartNet)
+    check(ccall((:tog_set_warm_start_net, libtog), Cint, (Ptr{Cvoid}, Ptr{Cvoid}), s.handle, net.handle))
+    return s
 end
 
 end # module
