@@ -47,6 +47,7 @@ enum tog_filter_kind { TOG_FILTER_NONE = 0, TOG_FILTER_DENSITY = 1, TOG_FILTER_S
  * without the network). */
 enum tog_warm_start { TOG_WARM_COLD = 0, TOG_WARM_PREVIOUS = 1, TOG_WARM_LEARNED = 2, TOG_WARM_EXTRAPOLATE = 3 };
 enum tog_filter_op { TOG_FILTER_J = 0, TOG_FILTER_JT = 1 };
+enum tog_projection_kind { TOG_PROJ_HEAVISIDE = 1, TOG_PROJ_SIGMOID = 2 };
 
 typedef struct tog_handle tog_handle;
 
@@ -146,6 +147,11 @@ int tog_filter_apply(tog_handle* h, int32_t op, const double* in, double* out);
  *      with move limit and eta = 1/2, bisection on lambda in [0, 1e9] to 1e-3) ---------- */
 /* x_new = clamp(x sqrt(max(0,-dc)/(dv lambda)), max(0,x-move), min(1,x+move)) with
  * sum(vol_weights . x_new) = volfrac.  Cell-sized host arrays. */
+/* HeavisideProjectionFun / SigmoidProjectionFun (src/Utilities/penalties.jl:75-96), the
+ * projections of ProjectedDensityFilterFun (src/CheqFilters/density_filter.jl:130-169):
+ * y = P(x) and dydx = P'(x) elementwise on cell-sized host arrays (beta >= 0).  Shares the
+ * filter's device scratch. */
+int tog_projection(tog_handle* h, int32_t kind, double beta, const double* x, double* y, double* dydx);
 int tog_oc_update(tog_handle* h, const double* x, const double* dc, const double* dv, const double* vol_weights,
                   double volfrac, double move, double* x_new, double* change, double* lambda);
 

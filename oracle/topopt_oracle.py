@@ -502,6 +502,51 @@ class SensFilter:
 # (l2-l1)/(l1+l2) <= 1e-3, volume measured on the physical (filtered) field).
 # --------------------------------------------------------------------------
 
+def heaviside_projection(x, beta):
+    """HeavisideProjectionFun (src/Utilities/penalties.jl:75-84): y = 1 - exp(-beta x)
+    + x exp(-beta); returns (y, dy/dx)."""
+    x = np.asarray(x, dtype=np.float64)
+    e = np.exp(-beta * x)
+    return 1.0 - e + x * np.exp(-beta), beta * e + np.exp(-beta)
+
+
+def sigmoid_projection(x, beta):
+    """SigmoidProjectionFun (penalties.jl:86-94): y = 1 / (1 + exp((beta + 1) (-x + 0.5)));
+    returns (y, dy/dx)."""
+    x = np.asarray(x, dtype=np.float64)
+    y = 1.0 / (1.0 + np.exp((beta + 1.0) * (-x + 0.5)))
+    return y, (beta + 1.0) * y * (1.0 - y)
+
+
+class ProjectedDensityFilter:
+    """ProjectedDensityFilterFun (src/CheqFilters/density_filter.jl:130-169):
+    y = postproj(J(preproj(x))); pullback by the chain rule (what Zygote computes
+    through the filter's rrule and the elementwise projections).  pre / post are
+    None or (function, beta)."""
+
+    def __init__(self, filt, pre=None, post=None):
+        self.filt, self.pre, self.post = filt, pre, post
+
+    def forward(self, x):
+        x = np.asarray(x, dtype=np.float64)
+        self.dpre = self.dpost = None
+        if self.pre is not None:
+            x, self.dpre = self.pre[0](x, self.pre[1])
+        y = self.filt.forward(x)
+        if self.post is not None:
+            y, self.dpost = self.post[0](y, self.post[1])
+        return y
+
+    def pullback(self, d):
+        d = np.asarray(d, dtype=np.float64)
+        if self.dpost is not None:
+            d = d * self.dpost
+        d = self.filt.pullback(d)
+        if self.dpre is not None:
+            d = d * self.dpre
+        return d
+
+
 def oc_update(x, dc, dv, vol_weights, volfrac, move=0.2, l1=0.0, l2=1e9, tol=1e-3):
     """x_new = clamp(x * sqrt(max(0,-dc)/(dv*lmid)), max(0,x-move), min(1,x+move));
     volume(x_new) = sum(vol_weights * x_new) compared with volfrac * sum(...)

@@ -244,3 +244,32 @@ def test_operator_tiling_and_chunking(tg, O, nels, kind, lz, monkeypatch):
         s(precision="fp32_ir")
         assert np.linalg.norm(s.u - ud) / np.linalg.norm(ud) < 1e-8
     s.close()
+
+
+@pytest.mark.parametrize("nels,kind", [((24, 10), "mbb"), ((10, 6, 4), "cantilever")])
+def test_projected_density_filter_matches_oracle(tg, O, nels, kind):
+    """ProjectedDensityFilterFun (density_filter.jl:130-169): the convenience form
+    (filter, then Heaviside beta = 10) and the three-argument form with a sigmoid
+    before and a Heaviside after the filter; forward and pullback at 1e-12."""
+    p, op = make(tg, O, nels, kind)
+    s = tg.FEASolver(tg.GB300Solver, p, xmin=1e-9, penalty=tg.PowerPenaltyFun(3.0))
+    rng = np.random.default_rng(4)
+    x = rng.uniform(0.05, 0.95, p.ncells)
+    w = rng.standard_normal(p.ncells)
+    rmin = 1.7
+    cases = [
+        (tg.ProjectedDensityFilterFun(s, rmin=rmin),
+         O.ProjectedDensityFilter(O.DensityFilter(op, rmin), post=(O.heaviside_projection, 10.0))),
+        (tg.ProjectedDensityFilterFun(tg.DensityFilterFun(s, rmin), tg.SigmoidProjectionFun(3.0),
+                                      tg.HeavisideProjectionFun(4.0)),
+         O.ProjectedDensityFilter(O.DensityFilter(op, rmin), pre=(O.sigmoid_projection, 3.0),
+                                  post=(O.heaviside_projection, 4.0))),
+    ]
+    for gpu, ref in cases:
+        y = gpu(tg.PseudoDensities(x)).x
+        yr = ref.forward(x)
+        assert rel(y, yr) < 1e-12
+        assert rel(gpu.pullback(w), ref.pullback(w)) < 1e-12
+    with pytest.raises(tg.TopOptError):
+        tg.ProjectedDensityFilterFun(s, rmin=rmin, projection=tg.HeavisideProjectionFun(-1.0))(x)
+    s.close()

@@ -149,3 +149,27 @@ def test_oc_update_volume_and_bounds(O):
     assert abs(w @ xn - 0.4) < 5e-3
     assert ch == pytest.approx(np.max(np.abs(xn - x)))
     assert steps > 10
+
+
+def test_oracle_projections_and_projected_filter_gradient(O):
+    """Heaviside / sigmoid projections and the projected density filter of the oracle:
+    derivatives and the chain-rule pullback against central finite differences."""
+    x = np.linspace(0.0, 1.0, 11)
+    for proj in (O.heaviside_projection, O.sigmoid_projection):
+        for beta in (1.0, 8.0):
+            y, dy = proj(x, beta)
+            fd = (proj(x + 1e-6, beta)[0] - proj(x - 1e-6, beta)[0]) / 2e-6
+            assert np.max(np.abs(fd - dy)) < 1e-6 * max(1.0, np.max(np.abs(dy)))
+    op = O.half_mbb((6, 4), (1.0, 1.0))
+    filt = O.DensityFilter(op, 1.6)
+    pf = O.ProjectedDensityFilter(filt, pre=(O.sigmoid_projection, 2.0), post=(O.heaviside_projection, 5.0))
+    rng = np.random.default_rng(0)
+    x0 = rng.uniform(0.1, 0.9, 24)
+    w = rng.standard_normal(24)
+    pf.forward(x0)
+    g = pf.pullback(w)
+    for i in range(0, 24, 5):
+        e = np.zeros(24)
+        e[i] = 1e-6
+        fd = (w @ pf.forward(x0 + e) - w @ pf.forward(x0 - e)) / 2e-6
+        assert abs(fd - g[i]) < 1e-6 * max(1.0, abs(g[i]))

@@ -15,11 +15,14 @@ from .topopt_api import (  # noqa: F401
     GB300FEASolver,
     GB300Solver,
     HalfMBB,
+    HeavisideProjectionFun,
     LoadedCantilever,
     PointLoadCantilever,
     PowerPenaltyFun,
+    ProjectedDensityFilterFun,
     PseudoDensities,
     SensFilterFun,
+    SigmoidProjectionFun,
     SIMPLoop,
     VolumeFun,
     WarmStartNet,

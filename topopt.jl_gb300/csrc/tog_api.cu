@@ -769,6 +769,26 @@ int nn_before_solve(tog_handle* h, bool use_net, bool use_du) {
     return TOG_OK;
 }
 
+// Projections of a density field and their derivatives (penalties.jl:75-96):
+//   Heaviside (kind 1): y = 1 - exp(-beta x) + x exp(-beta), y' = beta exp(-beta x) + exp(-beta)
+//   sigmoid   (kind 2): y = 1 / (1 + exp((beta + 1) (0.5 - x))), y' = (beta + 1) y (1 - y)
+__global__ void k_projection(int kind, double beta, const double* __restrict__ x, double* __restrict__ y,
+                             double* __restrict__ dy, long long n) {
+    const double eb = exp(-beta);
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const double xi = x[i];
+        if (kind == TOG_PROJ_HEAVISIDE) {
+            const double e = exp(-beta * xi);
+            y[i] = 1.0 - e + xi * eb;
+            dy[i] = beta * e + eb;
+        } else {
+            const double s = 1.0 / (1.0 + exp((beta + 1.0) * (0.5 - xi)));
+            y[i] = s;
+            dy[i] = (beta + 1.0) * s * (1.0 - s);
+        }
+    }
+}
+
 int do_solve(tog_handle* h, int prec, double rtol, double abstol, int maxit, int warm, tog_solve_stats* st) {
     TOG_TRY(refresh_scales(h));
     if (prec == TOG_FP64) return solve_fp64(h, rtol, abstol, maxit, warm, st);
@@ -1327,6 +1347,22 @@ int tog_filter_apply(tog_handle* h, int32_t op, const double* in, double* out) {
     TOG_CUDA(cudaMemcpyAsync(h->d_xnew, in, bytes, cudaMemcpyHostToDevice, h->stream));
     TOG_TRY(filter_dev(h, op, h->d_xnew, h->d_grad));
     TOG_CUDA(cudaMemcpyAsync(out, h->d_grad, bytes, cudaMemcpyDeviceToHost, h->stream));
+    TOG_CUDA(cudaStreamSynchronize(h->stream));
+    return TOG_OK;
+}
+
+int tog_projection(tog_handle* h, int32_t kind, double beta, const double* x, double* y, double* dydx) {
+    TOG_TRY(check_handle(h));
+    if (!x || !y || !dydx) return fail(TOG_ERR_ARG, "null array");
+    if (kind != TOG_PROJ_HEAVISIDE && kind != TOG_PROJ_SIGMOID) return fail(TOG_ERR_ARG, "unknown projection");
+    if (!std::isfinite(beta) || beta < 0) return fail(TOG_ERR_ARG, "projection steepness must be finite and >= 0");
+    const size_t bytes = h->ncells * sizeof(double);
+    TOG_CUDA(cudaMemcpyAsync(h->d_xnew, x, bytes, cudaMemcpyHostToDevice, h->stream));
+    k_projection<<<h->ew_blocks(h->ncells), kEwThreads, 0, h->stream>>>(kind, beta, h->d_xnew, h->d_grad, h->d_dc,
+                                                                       h->ncells);
+    TOG_CUDA(cudaGetLastError());
+    TOG_CUDA(cudaMemcpyAsync(y, h->d_grad, bytes, cudaMemcpyDeviceToHost, h->stream));
+    TOG_CUDA(cudaMemcpyAsync(dydx, h->d_dc, bytes, cudaMemcpyDeviceToHost, h->stream));
     TOG_CUDA(cudaStreamSynchronize(h->stream));
     return TOG_OK;
 }

@@ -359,6 +359,72 @@ class SensFilterFun(_NodeFilter):
         return self._apply(L.TOG_FILTER_J, delta)
 
 
+class HeavisideProjectionFun:
+    """y = 1 - exp(-beta x) + x exp(-beta) (penalties.jl:75-84)."""
+    kind = L.TOG_PROJ_HEAVISIDE
+
+    def __init__(self, beta):
+        self.beta = float(beta)
+
+
+class SigmoidProjectionFun:
+    """y = 1 / (1 + exp((beta + 1) (0.5 - x))) (penalties.jl:86-94)."""
+    kind = L.TOG_PROJ_SIGMOID
+
+    def __init__(self, beta):
+        self.beta = float(beta)
+
+
+def _project(solver, proj, x):
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    if x.shape != (solver.problem.ncells,):
+        raise ValueError("DimensionMismatch: one value per cell")
+    y, dy = np.empty_like(x), np.empty_like(x)
+    L.check(L.lib().tog_projection(solver.handle, proj.kind, proj.beta, L.dptr(x), L.dptr(y), L.dptr(dy)))
+    return y, dy
+
+
+class ProjectedDensityFilterFun:
+    """y = postproj(J(preproj(x))) (density_filter.jl:130-169): a density filter with a
+    projection before and/or after it; the pullback is the chain rule,
+    preproj'(x) * J'(postproj'(Jx~) * delta).  ProjectedDensityFilterFun(solver, rmin=...,
+    projection=HeavisideProjectionFun(10.0)) is the reference's convenience constructor
+    (filter, then the projection)."""
+
+    def __init__(self, filter_or_solver, preproj=None, postproj=None, *, rmin=None, projection="default"):
+        if isinstance(filter_or_solver, DensityFilterFun):
+            self.filter = filter_or_solver
+            self.preproj, self.postproj = preproj, postproj
+        else:
+            if rmin is None:
+                raise ValueError("ProjectedDensityFilterFun(solver; rmin, projection) needs rmin")
+            self.filter = DensityFilterFun(filter_or_solver, rmin)
+            self.preproj = None
+            self.postproj = HeavisideProjectionFun(10.0) if projection == "default" else projection
+        self.solver = self.filter.solver
+        self._d_pre = self._d_post = None
+
+    def __call__(self, x):
+        x = np.asarray(x.x if isinstance(x, PseudoDensities) else x, dtype=np.float64)
+        self._d_pre = None
+        if self.preproj is not None:
+            x, self._d_pre = _project(self.solver, self.preproj, x)
+        fx = self.filter(x).x
+        self._d_post = None
+        if self.postproj is not None:
+            fx, self._d_post = _project(self.solver, self.postproj, fx)
+        return PseudoDensities(fx)
+
+    def pullback(self, delta):
+        d = np.asarray(delta, dtype=np.float64)
+        if self._d_post is not None:
+            d = d * self._d_post
+        d = self.filter.pullback(d)
+        if self._d_pre is not None:
+            d = d * self._d_pre
+        return d
+
+
 def oc_update(solver, x, dc, dv, vol_weights, volfrac, move=0.2):
     """Optimality-criteria update (published method; no reference counterpart).
     Returns (x_new, change, lambda)."""
