@@ -48,6 +48,7 @@ enum tog_filter_kind { TOG_FILTER_NONE = 0, TOG_FILTER_DENSITY = 1, TOG_FILTER_S
 enum tog_warm_start { TOG_WARM_COLD = 0, TOG_WARM_PREVIOUS = 1, TOG_WARM_LEARNED = 2, TOG_WARM_EXTRAPOLATE = 3 };
 enum tog_filter_op { TOG_FILTER_J = 0, TOG_FILTER_JT = 1 };
 enum tog_projection_kind { TOG_PROJ_HEAVISIDE = 1, TOG_PROJ_SIGMOID = 2 };
+enum tog_element_state { TOG_ELEM_FREE = 0, TOG_ELEM_BLACK = 1, TOG_ELEM_WHITE = 2 };
 
 typedef struct tog_handle tog_handle;
 
@@ -143,15 +144,34 @@ int tog_filter_setup(tog_handle* h, double rmin);
  * op = TOG_FILTER_JT: y = J' x (DensityFilterFun pullback). Cell-sized host arrays. */
 int tog_filter_apply(tog_handle* h, int32_t op, const double* in, double* out);
 
-/* ---- optimality-criteria update (no reference counterpart: the published OC method
- *      with move limit and eta = 1/2, bisection on lambda in [0, 1e9] to 1e-3) ---------- */
-/* x_new = clamp(x sqrt(max(0,-dc)/(dv lambda)), max(0,x-move), min(1,x+move)) with
- * sum(vol_weights . x_new) = volfrac.  Cell-sized host arrays. */
 /* HeavisideProjectionFun / SigmoidProjectionFun (src/Utilities/penalties.jl:75-96), the
  * projections of ProjectedDensityFilterFun (src/CheqFilters/density_filter.jl:130-169):
  * y = P(x) and dydx = P'(x) elementwise on cell-sized host arrays (beta >= 0).  Shares the
  * filter's device scratch. */
 int tog_projection(tog_handle* h, int32_t kind, double beta, const double* x, double* y, double* dydx);
+
+/* ---- active-element mask: FixedElementProjectorFun (src/Functions/fixed_element.jl:13-159) ----
+ * state[e] (one byte per cell, cell order) is TOG_ELEM_FREE, TOG_ELEM_BLACK (density 1) or
+ * TOG_ELEM_WHITE (density 0); null makes every cell free.  A black-and-white cell cannot be
+ * expressed, the reference's ArgumentError for it belongs to the caller's constructor.  With a
+ * mask set, the OC update and the SIMP loop hold the fixed cells at their densities (their
+ * volume counts against volfrac, as the reference's VolumeFun on the projected field). */
+int tog_set_fixed_elements(tog_handle* h, const uint8_t* state);
+/* count(free) (get_free_variable_count, fixed_element.jl:95); ncells without a mask */
+int tog_free_variable_count(tog_handle* h, int64_t* nfree);
+/* rho = p(x_free) (fixed_element.jl:44-58): black 1, white 0, free cells copied from x_free
+ * in cell order.  TOG_ERR_ARG when nfree differs from the free count (the reference's
+ * ArgumentError).  Host arrays: x_free of nfree entries (may be null when nfree = 0), rho
+ * of ncells. */
+int tog_fixed_element_project(tog_handle* h, const double* x_free, int64_t nfree, double* rho);
+/* the rrule's pullback (fixed_element.jl:68-79): dx_free = drho[free]. */
+int tog_fixed_element_pullback(tog_handle* h, const double* drho, double* dx_free);
+
+/* ---- optimality-criteria update (no reference counterpart: the published OC method
+ *      with move limit and eta = 1/2, bisection on lambda in [0, 1e9] to 1e-3) ---------- */
+/* x_new = clamp(x sqrt(max(0,-dc)/(dv lambda)), max(0,x-move), min(1,x+move)) with
+ * sum(vol_weights . x_new) = volfrac.  Cell-sized host arrays.  Cells fixed by
+ * tog_set_fixed_elements keep their densities. */
 int tog_oc_update(tog_handle* h, const double* x, const double* dc, const double* dv, const double* vol_weights,
                   double volfrac, double move, double* x_new, double* change, double* lambda);
 

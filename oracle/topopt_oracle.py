@@ -547,15 +547,68 @@ class ProjectedDensityFilter:
         return d
 
 
-def oc_update(x, dc, dv, vol_weights, volfrac, move=0.2, l1=0.0, l2=1e9, tol=1e-3):
+class FixedElementProjector:
+    """FixedElementProjectorFun (src/Functions/fixed_element.jl:13-58): black cells at
+    density 1, white at 0, free cells copied from x_free in cell order; the pullback
+    returns the cotangent of the free cells (fixed_element.jl:68-79).  black / white are
+    boolean masks of length nel; both-black-and-white and length errors raise ValueError
+    (the reference's ArgumentError, fixed_element.jl:20-23, 46-50)."""
+
+    def __init__(self, nel, black, white):
+        black = np.asarray(black, dtype=bool)
+        white = np.asarray(white, dtype=bool)
+        if black.shape != (nel,):
+            raise ValueError("black must have length %d" % nel)
+        if white.shape != (nel,):
+            raise ValueError("white must have length %d" % nel)
+        if np.any(black & white):
+            raise ValueError("an element cannot be both black and white")
+        self.nel, self.black, self.white = nel, black, white
+        self.free = ~black & ~white
+
+    @classmethod
+    def from_cells(cls, nel, black_cells, white_cells):
+        """get_fixed_element_projector(nel, black_cells, white_cells)
+        (fixed_element.jl:150-159), with 0-based cell indices."""
+        black = np.zeros(nel, dtype=bool)
+        white = np.zeros(nel, dtype=bool)
+        black[np.asarray(black_cells, dtype=np.int64)] = True
+        white[np.asarray(white_cells, dtype=np.int64)] = True
+        return cls(nel, black, white)
+
+    @property
+    def nfree(self):
+        return int(np.count_nonzero(self.free))
+
+    def __call__(self, x_free):
+        x_free = np.asarray(x_free, dtype=np.float64)
+        if x_free.shape != (self.nfree,):
+            raise ValueError("x_free length (%d) must match number of free elements (%d)"
+                             % (x_free.size, self.nfree))
+        rho = np.empty(self.nel)
+        rho[self.black] = 1.0
+        rho[self.white] = 0.0
+        rho[self.free] = x_free
+        return rho
+
+    def pullback(self, d):
+        return np.asarray(d, dtype=np.float64)[self.free]
+
+
+def oc_update(x, dc, dv, vol_weights, volfrac, move=0.2, l1=0.0, l2=1e9, tol=1e-3, fixed=None):
     """x_new = clamp(x * sqrt(max(0,-dc)/(dv*lmid)), max(0,x-move), min(1,x+move));
     volume(x_new) = sum(vol_weights * x_new) compared with volfrac * sum(...)
     on the same weights' total (vol_weights = colsum(J) / ncells for the density
-    filter, 1/ncells without a filter).  Returns (x_new, change, lmid, steps)."""
+    filter, 1/ncells without a filter).  fixed (a FixedElementProjector) holds its
+    black / white cells at 1 / 0: their bounds collapse onto that value, and their
+    volume counts against volfrac.  Returns (x_new, change, lmid, steps)."""
     x = np.asarray(x, dtype=np.float64)
     B = x * np.sqrt(np.maximum(0.0, -dc) / dv)
     lo = np.maximum(0.0, x - move)
     hi = np.minimum(1.0, x + move)
+    if fixed is not None:
+        lo[fixed.black] = hi[fixed.black] = 1.0
+        lo[fixed.white] = hi[fixed.white] = 0.0
     steps = 0
     xnew = x
     while (l2 - l1) / (l1 + l2) > tol:
@@ -574,7 +627,7 @@ def oc_update(x, dc, dv, vol_weights, volfrac, move=0.2, l1=0.0, l2=1e9, tol=1e-
 
 
 def simp_iteration(st: FEAState, x, filt, volfrac, move=0.2, solve="direct",
-                   rtol=1e-10, maxiter=100000, vol_weights=None):
+                   rtol=1e-10, maxiter=100000, vol_weights=None, fixed=None):
     """One design iteration: filter -> solve -> compliance/sens -> filter pullback
     -> OC (docs/tutorials/simp.qmd:86-114 with OC in place of MMA)."""
     xf = filt.forward(x) if filt is not None else x.copy()
@@ -597,6 +650,6 @@ def simp_iteration(st: FEAState, x, filt, volfrac, move=0.2, solve="direct",
             vol_weights = np.asarray(filt.J.sum(axis=0)).ravel() / n
         else:
             vol_weights = np.full(n, 1.0 / n)
-    xnew, change, lam, steps = oc_update(x, dc, dv, vol_weights, volfrac, move)
+    xnew, change, lam, steps = oc_update(x, dc, dv, vol_weights, volfrac, move, fixed=fixed)
     return dict(x_new=xnew, xf=xf, u=u, c=c, g=g, dc=dc, dv=dv, change=change,
                 lam=lam, oc_steps=steps, cg_iters=its)

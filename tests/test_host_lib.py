@@ -82,3 +82,26 @@ def test_config3_problem_set(tg):
     assert P["rmin"].min() >= 1.5 and P["rmin"].max() <= 3.0
     Q = tg.config3_problems(256, seed=0)
     assert all(np.array_equal(P[k], Q[k]) for k in ("nelx", "nely", "load_j", "volfrac", "rmin"))
+
+
+def test_fixed_element_projector_host_logic(tg):
+    """FixedElementProjectorFun's constructor and queries are host logic
+    (fixed_element.jl:19-27, 88-95, 127-159): no device call."""
+    black = np.zeros(10, bool)
+    black[:3] = True
+    white = np.zeros(10, bool)
+    white[7:] = True
+    p = tg.FixedElementProjectorFun(10, black, white)
+    assert tg.get_free_variable_count(p) == 4
+    assert tg.get_free_variables(p).tolist() == [False] * 3 + [True] * 4 + [False] * 3
+    with pytest.raises(ValueError):
+        tg.FixedElementProjectorFun(5, np.array([1, 1, 1, 0, 0], bool), np.array([0, 0, 1, 1, 1], bool))
+    with pytest.raises(ValueError):
+        tg.FixedElementProjectorFun(5, np.zeros(5, bool), np.zeros(6, bool))
+    q = tg.get_fixed_element_projector(100, range(0, 10), range(90, 100))
+    assert (tg.get_free_variable_count(q), int(q.black.sum()), int(q.white.sum())) == (80, 10, 10)
+    prob = tg.PointLoadCantilever((10, 6), (1.0, 1.0))
+    r = tg.get_fixed_element_projector(prob, range(10), [])
+    assert r.nel == 60 and tg.get_free_variable_count(r) == 50
+    with pytest.raises(RuntimeError):   # the projection itself runs on a solver's device
+        r(np.full(50, 0.5))

@@ -173,3 +173,65 @@ def test_oracle_projections_and_projected_filter_gradient(O):
         e[i] = 1e-6
         fd = (w @ pf.forward(x0 + e) - w @ pf.forward(x0 - e)) / 2e-6
         assert abs(fd - g[i]) < 1e-6 * max(1.0, abs(g[i]))
+
+
+# ---------------------------------------------------------------- FixedElementProjectorFun
+def _mask(n, idx):
+    m = np.zeros(n, dtype=bool)
+    m[list(idx)] = True
+    return m
+
+
+def test_fixed_element_projector_pins(O):
+    """The known answers of test/Functions/test_fixed_element.jl:22-236 (0-based cells)."""
+    black, white = _mask(10, range(0, 3)), _mask(10, range(7, 10))
+    p = O.FixedElementProjector(10, black, white)
+    assert p.nfree == 4
+    assert p.free.tolist() == [False, False, False, True, True, True, True, False, False, False]
+    with pytest.raises(ValueError):   # element 3 both black and white
+        O.FixedElementProjector(5, _mask(5, range(0, 3)), _mask(5, range(2, 5)))
+    with pytest.raises(ValueError):   # mismatched lengths
+        O.FixedElementProjector(5, np.zeros(5, bool), np.zeros(6, bool))
+    rho = p(np.array([0.0, 0.25, 0.5, 0.75]))
+    assert rho.tolist() == [1.0, 1.0, 1.0, 0.0, 0.25, 0.5, 0.75, 0.0, 0.0, 0.0]
+    for bad in (np.zeros(2), np.zeros(5)):
+        with pytest.raises(ValueError):
+            p(bad)
+    # sum(p(x)) has gradient ones; sum(abs2, p(x)) has gradient 2 x (finite differences)
+    x = np.array([0.1, 0.2, 0.3, 0.4])
+    assert np.allclose(p.pullback(np.ones(10)), np.ones(4), rtol=1e-10)
+    h = 1e-6
+    fd = [(np.sum(p(x + h * np.eye(4)[i]) ** 2) - np.sum(p(x) ** 2)) / h for i in range(4)]
+    assert np.allclose(p.pullback(2 * p(x)), fd, rtol=1e-5)
+    # the pullback keeps only the free cells (free: element 3 of 5)
+    q = O.FixedElementProjector(5, _mask(5, range(0, 2)), _mask(5, range(3, 5)))
+    assert q.pullback(np.ones(5)).tolist() == [1.0]
+    # identity without fixed cells
+    x5 = np.array([0.0, 0.25, 0.5, 0.75, 1.0])
+    assert O.FixedElementProjector(5, np.zeros(5, bool), np.zeros(5, bool))(x5).tolist() == x5.tolist()
+    # edge cases: all black, all white, none fixed, one element
+    assert O.FixedElementProjector(5, np.ones(5, bool), np.zeros(5, bool))(np.zeros(0)).tolist() == [1.0] * 5
+    assert O.FixedElementProjector(5, np.zeros(5, bool), np.ones(5, bool))(np.zeros(0)).tolist() == [0.0] * 5
+    assert O.FixedElementProjector(1, np.zeros(1, bool), np.zeros(1, bool))(np.array([0.5])).tolist() == [0.5]
+    # get_fixed_element_projector by nel
+    assert O.FixedElementProjector.from_cells(100, [], []).nfree == 100
+    g = O.FixedElementProjector.from_cells(100, range(0, 10), range(90, 100))
+    assert (g.nfree, int(g.black.sum()), int(g.white.sum())) == (80, 10, 10)
+
+
+def test_oc_holds_fixed_cells(O):
+    """OC with an active-element mask: fixed cells keep 1 / 0 exactly, the volume of the
+    black cells counts against volfrac, and free cells follow the unmasked rule with the
+    new multiplier."""
+    rng = np.random.default_rng(2)
+    n = 200
+    fx = O.FixedElementProjector.from_cells(n, range(0, 20), range(180, 200))
+    x = fx(rng.uniform(0.1, 0.9, fx.nfree))
+    dc = -rng.uniform(0.1, 2.0, n)
+    w = np.full(n, 1.0 / n)
+    xn, ch, lam, _ = O.oc_update(x, dc, w, w, 0.4, 0.2, fixed=fx)
+    assert np.all(xn[fx.black] == 1.0) and np.all(xn[fx.white] == 0.0)
+    assert abs(float(w @ xn) - 0.4) < 2e-3
+    B = x * np.sqrt(-dc / w)
+    free = np.clip(B / np.sqrt(lam), np.maximum(0, x - 0.2), np.minimum(1, x + 0.2))
+    assert np.array_equal(xn[fx.free], free[fx.free])

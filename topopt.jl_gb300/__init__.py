@@ -12,6 +12,7 @@ from .topopt_api import (  # noqa: F401
     ComplianceFun,
     DensityFilterFun,
     FEASolver,
+    FixedElementProjectorFun,
     GB300FEASolver,
     GB300Solver,
     HalfMBB,
@@ -29,6 +30,9 @@ from .topopt_api import (  # noqa: F401
     cell_dofs,
     config3_problems,
     element_stiffness,
+    get_fixed_element_projector,
+    get_free_variable_count,
+    get_free_variables,
     grid_counts,
     node_dofs,
     oc_update,

@@ -12,6 +12,7 @@ LIB_PATH = os.path.join(HERE, "libtopopt_gb300.so")
 TOG_OK, TOG_ERR_ARG, TOG_ERR_CUDA, TOG_NOT_CONVERGED, TOG_BREAKDOWN, TOG_ERR_STATE, TOG_ERR_OOM = range(7)
 TOG_FP64, TOG_FP32_IR = 0, 1
 TOG_PROJ_HEAVISIDE, TOG_PROJ_SIGMOID = 1, 2
+TOG_ELEM_FREE, TOG_ELEM_BLACK, TOG_ELEM_WHITE = 0, 1, 2
 TOG_FILTER_NONE, TOG_FILTER_DENSITY, TOG_FILTER_SENS = 0, 1, 2
 TOG_FILTER_J, TOG_FILTER_JT = 0, 1
 
@@ -99,6 +100,10 @@ SIGNATURES = {
     "tog_record_next_step": (C.c_int, [_H, C.c_void_p, C.c_void_p]),
     "tog_record_status": (C.c_int, [_H, _I32]),
     "tog_projection": (C.c_int, [_H, C.c_int32, C.c_double, _D, _D, _D]),
+    "tog_set_fixed_elements": (C.c_int, [_H, C.c_void_p]),
+    "tog_free_variable_count": (C.c_int, [_H, _I64]),
+    "tog_fixed_element_project": (C.c_int, [_H, _D, C.c_int64, _D]),
+    "tog_fixed_element_pullback": (C.c_int, [_H, _D, _D]),
     "tog_oc_update_noalloc": (C.c_int, [C.c_int64, _D, _D, _D, _D, C.c_double, C.c_double, _D, _D, C.c_void_p]),
 }
 

@@ -117,6 +117,10 @@ struct tog_handle {
     double *d_x = nullptr, *d_xnew = nullptr, *d_dc = nullptr, *d_dv = nullptr, *d_w = nullptr, *d_grad = nullptr,
            *d_B = nullptr;
     bool simp_ready = false;
+    // active-element mask (FixedElementProjectorFun): position of each cell in x_free,
+    // -1 black, -2 white; null when every cell is free
+    int* d_fpos = nullptr;
+    long long nfree = 0;
     // learned warm start (3D): network, previous-iteration state and recording hook
     tog_nn* net = nullptr;
     double* d_vars_prev = nullptr;   // physical densities of the previous design iteration
@@ -843,9 +847,10 @@ int build_oc_graph(tog_handle* h) {
     TOG_CUDA(cudaStreamBeginCapture(h->own, cudaStreamCaptureModeThreadLocal));
     const int nb = h->ew_blocks(h->ncells);
     for (int i = 0; i < kOcMaxSteps; ++i)
-        k_oc_step<<<nb, kEwThreads, 0, h->own>>>(h->d_x, h->d_B, h->d_w, h->ncells, h->d_oc, h->d_partials);
+        k_oc_step<<<nb, kEwThreads, 0, h->own>>>(h->d_x, h->d_B, h->d_w, h->ncells, h->d_oc, h->d_partials,
+                                                 h->d_fpos);
     k_oc_final<<<nb, kEwThreads, 0, h->own>>>(h->d_x, h->d_B, h->d_xnew, h->ncells, h->d_oc, h->d_partials,
-                                               h->d_w);
+                                               h->d_w, h->d_fpos);
     TOG_CUDA(cudaStreamEndCapture(h->own, &g));
     TOG_CUDA(cudaGraphInstantiate(&h->g_oc, g, 0));
     cudaGraphDestroy(g);
@@ -1182,7 +1187,7 @@ int tog_destroy(tog_handle* h) {
                     h->d_e32,     h->d_dinv64,  h->d_dinv32,  h->d_nodal,   h->d_st64,    h->d_st32,
                     h->d_oc,      h->d_partials, h->d_cnt,    h->d_scalar,  h->d_invW,    h->d_soff,
                     h->d_sw,      h->d_vars_prev, h->d_uprev, h->d_du_last, h->d_nn_in, h->d_nn_out, h->d_nn_sc,
-                    h->d_nn_part, h->d_nn_cnt};
+                    h->d_nn_part, h->d_nn_cnt, h->d_fpos};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (int i = 0; i < 6; ++i)
@@ -1367,6 +1372,93 @@ int tog_projection(tog_handle* h, int32_t kind, double beta, const double* x, do
     return TOG_OK;
 }
 
+int tog_set_fixed_elements(tog_handle* h, const uint8_t* state) {
+    TOG_TRY(check_handle(h));
+    if (!state) {   // every cell free
+        if (h->d_fpos) {
+            TOG_CUDA(cudaStreamSynchronize(h->stream));
+            cudaFree(h->d_fpos);
+            h->d_fpos = nullptr;
+        }
+        h->nfree = h->ncells;
+    } else {
+        if (h->ncells >= (1LL << 31)) return fail(TOG_ERR_ARG, "the active-element mask needs fewer than 2^31 cells");
+        std::vector<int> pos(h->ncells);
+        long long nf = 0;
+        for (long long e = 0; e < h->ncells; ++e) {
+            if (state[e] > TOG_ELEM_WHITE)
+                return fail(TOG_ERR_ARG, "element state must be 0 (free), 1 (black) or 2 (white), cell " +
+                                             std::to_string(e) + " has " + std::to_string((int)state[e]));
+            pos[e] = state[e] == TOG_ELEM_FREE ? (int)nf++ : (state[e] == TOG_ELEM_BLACK ? -1 : -2);
+        }
+        if (!h->d_fpos) TOG_TRY(dalloc(&h->d_fpos, h->ncells));
+        TOG_CUDA(cudaMemcpyAsync(h->d_fpos, pos.data(), h->ncells * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+        TOG_CUDA(cudaStreamSynchronize(h->stream));
+        h->nfree = nf;
+    }
+    // the OC graph holds the mask pointer: capture it again on the next update
+    if (h->g_oc) {
+        TOG_CUDA(cudaStreamSynchronize(h->stream));
+        cudaGraphExecDestroy(h->g_oc);
+        h->g_oc = nullptr;
+    }
+    if (h->d_fpos && h->simp_ready) {   // an active loop's design follows the new mask at once
+        k_fixed_pin<<<h->ew_blocks(h->ncells), kEwThreads, 0, h->stream>>>(h->d_x, h->d_fpos, h->ncells);
+        TOG_LAUNCHED(1);
+        TOG_CUDA(cudaGetLastError());
+        TOG_CUDA(cudaStreamSynchronize(h->stream));
+    }
+    return TOG_OK;
+}
+
+int tog_free_variable_count(tog_handle* h, int64_t* nfree) {
+    TOG_TRY(check_handle(h));
+    if (!nfree) return fail(TOG_ERR_ARG, "null output");
+    *nfree = h->d_fpos ? h->nfree : h->ncells;
+    return TOG_OK;
+}
+
+int tog_fixed_element_project(tog_handle* h, const double* x_free, int64_t nfree, double* rho) {
+    TOG_TRY(check_handle(h));
+    const long long nf = h->d_fpos ? h->nfree : h->ncells;
+    if (nfree != nf)
+        return fail(TOG_ERR_ARG, "x_free length (" + std::to_string((long long)nfree) +
+                                     ") must match number of free elements (" + std::to_string(nf) + ")");
+    if (!rho || (nf > 0 && !x_free)) return fail(TOG_ERR_ARG, "null array");
+    if (nf > 0)
+        TOG_CUDA(cudaMemcpyAsync(h->d_xnew, x_free, nf * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    if (h->d_fpos) {
+        k_fixed_project<<<h->ew_blocks(h->ncells), kEwThreads, 0, h->stream>>>(h->d_xnew, h->d_fpos, h->d_grad,
+                                                                              h->ncells);
+        TOG_LAUNCHED(1);
+        TOG_CUDA(cudaGetLastError());
+        TOG_CUDA(cudaMemcpyAsync(rho, h->d_grad, h->ncells * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    } else {
+        TOG_CUDA(cudaMemcpyAsync(rho, h->d_xnew, h->ncells * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    }
+    TOG_CUDA(cudaStreamSynchronize(h->stream));
+    return TOG_OK;
+}
+
+int tog_fixed_element_pullback(tog_handle* h, const double* drho, double* dx_free) {
+    TOG_TRY(check_handle(h));
+    const long long nf = h->d_fpos ? h->nfree : h->ncells;
+    if (!drho || (nf > 0 && !dx_free)) return fail(TOG_ERR_ARG, "null array");
+    TOG_CUDA(cudaMemcpyAsync(h->d_xnew, drho, h->ncells * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    if (h->d_fpos) {
+        k_fixed_pullback<<<h->ew_blocks(h->ncells), kEwThreads, 0, h->stream>>>(h->d_xnew, h->d_fpos, h->d_grad,
+                                                                               h->ncells);
+        TOG_LAUNCHED(1);
+        TOG_CUDA(cudaGetLastError());
+        if (nf > 0)
+            TOG_CUDA(cudaMemcpyAsync(dx_free, h->d_grad, nf * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    } else {
+        TOG_CUDA(cudaMemcpyAsync(dx_free, h->d_xnew, nf * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    }
+    TOG_CUDA(cudaStreamSynchronize(h->stream));
+    return TOG_OK;
+}
+
 int tog_oc_update(tog_handle* h, const double* x, const double* dc, const double* dv, const double* vol_weights,
                   double volfrac, double move, double* x_new, double* change, double* lambda) {
     TOG_TRY(check_handle(h));
@@ -1397,6 +1489,11 @@ int tog_simp_init(tog_handle* h, int32_t filter_kind, double rmin, double volfra
     h->move = move;
     const size_t bytes = h->ncells * sizeof(double);
     TOG_CUDA(cudaMemcpyAsync(h->d_x, x0, bytes, cudaMemcpyHostToDevice, h->stream));
+    if (h->d_fpos) {   // fixed cells start (and stay) at their densities
+        k_fixed_pin<<<h->ew_blocks(h->ncells), kEwThreads, 0, h->stream>>>(h->d_x, h->d_fpos, h->ncells);
+        TOG_LAUNCHED(1);
+        TOG_CUDA(cudaGetLastError());
+    }
     // dv = d(volume fraction)/dx; for the density filter dv = J' (1/n) (volume.jl:59-67 + filter rrule),
     // which is also the weight of x in the filtered volume used by the OC bisection.
     std::vector<double> inv(h->ncells, 1.0 / (double)h->ncells);
@@ -1525,6 +1622,11 @@ int tog_set_design(tog_handle* h, const double* x) {
     TOG_TRY(check_handle(h));
     if (!x) return fail(TOG_ERR_ARG, "null input");
     TOG_CUDA(cudaMemcpyAsync(h->d_x, x, h->ncells * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    if (h->d_fpos) {
+        k_fixed_pin<<<h->ew_blocks(h->ncells), kEwThreads, 0, h->stream>>>(h->d_x, h->d_fpos, h->ncells);
+        TOG_LAUNCHED(1);
+        TOG_CUDA(cudaGetLastError());
+    }
     return TOG_OK;
 }
 

@@ -698,7 +698,18 @@ __global__ void __launch_bounds__(256) k_filt_cone_T(const double* __restrict__ 
 // ---------------------------------------------------------------------------
 // OC update (FP64).  B_e = x_e sqrt(max(0,-dc_e)/dv_e); bisection on lambda
 // with x_new = clamp(B_e / sqrt(lambda), max(0,x-move), min(1,x+move)).
+// fpos (optional) is the active-element mask: fpos[e] < 0 pins cell e (-1 black at
+// density 1, -2 white at density 0) by collapsing its bounds onto that value.
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ double oc_new(double xe, double b, double move, const int* __restrict__ fpos,
+                                         long long e) {
+    double lo = fmax(0.0, xe - move), hi = fmin(1.0, xe + move);
+    if (fpos) {
+        const int p = fpos[e];
+        if (p < 0) lo = hi = (p == -1) ? 1.0 : 0.0;
+    }
+    return fmin(hi, fmax(lo, b));
+}
 __global__ void __launch_bounds__(256) k_oc_prep(const double* __restrict__ x, const double* __restrict__ dc,
                                                  const double* __restrict__ dv, double* __restrict__ B, long long n,
                                                  OcState* oc, double l1, double l2, double tol, double target,
@@ -722,7 +733,7 @@ __global__ void __launch_bounds__(256) k_oc_prep(const double* __restrict__ x, c
 
 __global__ void __launch_bounds__(256) k_oc_step(const double* __restrict__ x, const double* __restrict__ B,
                                                  const double* __restrict__ w, long long n, OcState* oc,
-                                                 double* partials) {
+                                                 double* partials, const int* __restrict__ fpos) {
     if (oc->done) return;
     const double lmid = 0.5 * (oc->l2 + oc->l1);
     const double s = 1.0 / sqrt(lmid);
@@ -730,8 +741,7 @@ __global__ void __launch_bounds__(256) k_oc_step(const double* __restrict__ x, c
     double acc = 0.0;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
          e += (long long)gridDim.x * blockDim.x) {
-        const double xe = x[e];
-        const double xn = fmin(fmin(1.0, xe + move), fmax(fmax(0.0, xe - move), B[e] * s));
+        const double xn = oc_new(x[e], B[e] * s, move, fpos, e);
         acc = fma(w[e], xn, acc);
     }
     double v[1] = {acc}, tot[1];
@@ -750,7 +760,8 @@ __global__ void __launch_bounds__(256) k_oc_step(const double* __restrict__ x, c
 
 __global__ void __launch_bounds__(256) k_oc_final(const double* __restrict__ x, const double* __restrict__ B,
                                                   double* __restrict__ xnew, long long n, OcState* oc,
-                                                  double* partials, const double* __restrict__ w) {
+                                                  double* partials, const double* __restrict__ w,
+                                                  const int* __restrict__ fpos) {
     const double lmid = 0.5 * (oc->l2 + oc->l1);
     const double s = 1.0 / sqrt(lmid);
     const double move = oc->move;
@@ -758,7 +769,7 @@ __global__ void __launch_bounds__(256) k_oc_final(const double* __restrict__ x, 
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
          e += (long long)gridDim.x * blockDim.x) {
         const double xe = x[e];
-        const double xn = fmin(fmin(1.0, xe + move), fmax(fmax(0.0, xe - move), B[e] * s));
+        const double xn = oc_new(xe, B[e] * s, move, fpos, e);
         xnew[e] = xn;
         mx = fmax(mx, fabs(xn - xe));
         vol = fma(w[e], xn, vol);
@@ -773,6 +784,38 @@ __global__ void __launch_bounds__(256) k_oc_final(const double* __restrict__ x, 
     double v2[1] = {vol}, tot2[1];
     if (grid_reduce_last<1>(v2, partials + 2 * gridDim.x, &oc->cnt[2], tot2)) {
         if (threadIdx.x == 0) oc->vol = tot2[0];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// FixedElementProjectorFun (src/Functions/fixed_element.jl:44-79) on the device.
+// fpos[e] >= 0 is the position of free cell e in x_free (free cells in cell order),
+// -1 a black cell (density 1), -2 a white cell (density 0).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_fixed_project(const double* __restrict__ xf, const int* __restrict__ fpos,
+                                                       double* __restrict__ rho, long long n) {
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int p = fpos[e];
+        rho[e] = p >= 0 ? xf[p] : (p == -1 ? 1.0 : 0.0);
+    }
+}
+// pullback: the cotangent of the free cells, in x_free order (fixed cells receive none)
+__global__ void __launch_bounds__(256) k_fixed_pullback(const double* __restrict__ drho,
+                                                        const int* __restrict__ fpos, double* __restrict__ dxf,
+                                                        long long n) {
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int p = fpos[e];
+        if (p >= 0) dxf[p] = drho[e];
+    }
+}
+// hold the fixed cells of a full design vector at their densities
+__global__ void __launch_bounds__(256) k_fixed_pin(double* __restrict__ x, const int* __restrict__ fpos, long long n) {
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int p = fpos[e];
+        if (p < 0) x[e] = (p == -1) ? 1.0 : 0.0;
     }
 }
 

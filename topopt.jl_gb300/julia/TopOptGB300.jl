@@ -33,6 +33,7 @@ using Ferrite
 
 export GB300Solver, GB300FEASolver, GB300DensityFilter, GB300SensFilter, oc_update!, simp_step!
 export BatchedSIMP, batch_step!, batch_results, WarmStartNet, attach_network!
+export GB300FixedElementProjector, clear_fixed_elements!, GB300ProjectedDensityFilter
 
 const libtog = joinpath(@__DIR__, "..", "libtopopt_gb300.so")
 
@@ -224,6 +225,96 @@ function oc_update!(xnew::Vector{Float64}, s::GB300FEASolver, x, dc, dv, w; volf
                 s.handle, Vector{Float64}(x), Vector{Float64}(dc), Vector{Float64}(dv), Vector{Float64}(w),
                 Float64(volfrac), Float64(move), xnew, ch, lam))
     return ch[], lam[]
+end
+
+_proj_kind(::TopOpt.Utilities.HeavisideProjectionFun) = Int32(1)
+_proj_kind(::TopOpt.Utilities.SigmoidProjectionFun) = Int32(2)
+function _project(s::GB300FEASolver, P, x::AbstractVector)
+    y, dy = zeros(length(x)), zeros(length(x))
+    check(ccall((:tog_projection, libtog), Cint,
+                (Ptr{Cvoid}, Int32, Float64, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}),
+                s.handle, _proj_kind(P), Float64(P.β), Vector{Float64}(x), y, dy))
+    return y, dy
+end
+
+"""
+    ProjectedDensityFilterFun(solver::GB300FEASolver; rmin, projection=HeavisideProjectionFun(10.0))
+    GB300ProjectedDensityFilter(filter::GB300DensityFilter, preproj, postproj)
+
+ProjectedDensityFilterFun (src/CheqFilters/density_filter.jl:129-169) on the device: the
+reference type holds a concrete `DensityFilterFun`, so the GB300 filter comes with its own
+wrapper.  The projections (Heaviside / sigmoid, `src/Utilities/penalties.jl:75-94`) run
+through `tog_projection`; the rrule is the chain rule through both projections and J'.
+"""
+struct GB300ProjectedDensityFilter{TF<:GB300DensityFilter,TP1,TP2} <: AbstractDensityFilter
+    filter::TF
+    preproj::TP1
+    postproj::TP2
+end
+function TopOpt.CheqFilters.ProjectedDensityFilterFun(s::GB300FEASolver; rmin,
+                                                      projection=TopOpt.Utilities.HeavisideProjectionFun(10.0))
+    return GB300ProjectedDensityFilter(DensityFilterFun(s, rmin), nothing, projection)
+end
+function _projected_forward(f::GB300ProjectedDensityFilter, x::AbstractVector)
+    s = f.filter.solver
+    x1, d1 = f.preproj === nothing ? (Vector{Float64}(x), nothing) : _project(s, f.preproj, x)
+    fx = _filter_apply(s, 0, x1)
+    y, d2 = f.postproj === nothing ? (fx, nothing) : _project(s, f.postproj, fx)
+    return y, d1, d2
+end
+(f::GB300ProjectedDensityFilter)(x::PseudoDensities{I,P}) where {I,P} =
+    PseudoDensities{I,P,true}(_projected_forward(f, x.x)[1])
+function ChainRulesCore.rrule(f::GB300ProjectedDensityFilter, x::PseudoDensities{I,P}) where {I,P}
+    y, d1, d2 = _projected_forward(f, x.x)
+    return PseudoDensities{I,P,true}(y), Δ -> begin
+        _Δ = ChainRulesCore.unthunk(Δ)
+        _Δ = hasproperty(_Δ, :x) ? _Δ.x : _Δ
+        g = d2 === nothing ? Vector{Float64}(_Δ) : _Δ .* d2
+        g = _filter_apply(f.filter.solver, 1, g)
+        d1 === nothing || (g = g .* d1)
+        (NoTangent(), Tangent{typeof(x)}(; x=g))
+    end
+end
+
+"""
+    GB300FixedElementProjector(solver, p::FixedElementProjectorFun)
+
+FixedElementProjectorFun (src/Functions/fixed_element.jl:13-79) on the device of `solver`:
+calling it projects x_free (black 1, white 0, free cells copied), its rrule gathers the
+free cells' cotangent.  Constructing it sets the solver's active-element mask, so
+`simp_step!` and `oc_update!` hold the fixed cells at their densities.
+"""
+struct GB300FixedElementProjector{TS<:GB300FEASolver}
+    solver::TS
+    proj::TopOpt.Functions.FixedElementProjectorFun
+end
+function GB300FixedElementProjector(s::GB300FEASolver, p::TopOpt.Functions.FixedElementProjectorFun)
+    p.nel == getncells(s.problem) || throw(DimensionMismatch("projector and problem cell counts differ"))
+    state = zeros(UInt8, p.nel)
+    state[p.black] .= 0x01
+    state[p.white] .= 0x02
+    check(ccall((:tog_set_fixed_elements, libtog), Cint, (Ptr{Cvoid}, Ptr{UInt8}), s.handle, state))
+    return GB300FixedElementProjector{typeof(s)}(s, p)
+end
+clear_fixed_elements!(s::GB300FEASolver) =
+    check(ccall((:tog_set_fixed_elements, libtog), Cint, (Ptr{Cvoid}, Ptr{UInt8}), s.handle, C_NULL))
+function (g::GB300FixedElementProjector)(x_free::AbstractVector)
+    nf = count(g.proj.free)
+    length(x_free) == nf || throw(ArgumentError(
+        "x_free length ($(length(x_free))) must match number of free elements ($nf)"))
+    ρ = zeros(g.proj.nel)
+    check(ccall((:tog_fixed_element_project, libtog), Cint, (Ptr{Cvoid}, Ptr{Float64}, Int64, Ptr{Float64}),
+                g.solver.handle, Vector{Float64}(x_free), Int64(nf), ρ))
+    return ρ
+end
+function ChainRulesCore.rrule(g::GB300FixedElementProjector, x_free::AbstractVector)
+    y = g(x_free)
+    return y, Δ -> begin
+        dx = zeros(count(g.proj.free))
+        check(ccall((:tog_fixed_element_pullback, libtog), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}),
+                    g.solver.handle, Vector{Float64}(ChainRulesCore.unthunk(Δ)), dx))
+        (NoTangent(), dx)
+    end
 end
 
 mutable struct IterStats

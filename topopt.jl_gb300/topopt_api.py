@@ -425,6 +425,110 @@ class ProjectedDensityFilterFun:
         return d
 
 
+class FixedElementProjectorFun:
+    """FixedElementProjectorFun(nel, black, white) (src/Functions/fixed_element.jl:13-58):
+    maps the free design variables to the full density vector, black cells at 1, white at
+    0, free cells copied in cell order; the pullback passes the cotangent of the free cells
+    only (fixed_element.jl:68-79).  black / white are boolean masks of length nel (the
+    reference's BitVectors); a cell that is both, or a mask of another length, raises
+    ValueError (the reference's ArgumentError).
+
+    The projection runs on the device of the solver it is attached to
+    (get_fixed_element_projector(solver, ...) or attach(solver)).  Attaching also sets
+    that solver's active-element mask, so its SIMPLoop and oc_update hold the fixed cells
+    at their densities."""
+
+    def __init__(self, nel, black, white):
+        nel = int(nel)
+        black = np.asarray(black, dtype=bool)
+        white = np.asarray(white, dtype=bool)
+        if black.shape != (nel,):
+            raise ValueError("black must have length %d" % nel)
+        if white.shape != (nel,):
+            raise ValueError("white must have length %d" % nel)
+        if np.any(black & white):
+            raise ValueError("an element cannot be both black and white")
+        self.nel, self.black, self.white = nel, black, white
+        self.free = ~black & ~white
+        self.solver = None
+
+    def attach(self, solver):
+        if solver.problem.ncells != self.nel:
+            raise ValueError("DimensionMismatch: the projector has %d cells, the problem %d"
+                             % (self.nel, solver.problem.ncells))
+        state = np.zeros(self.nel, dtype=np.uint8)
+        state[self.black] = L.TOG_ELEM_BLACK
+        state[self.white] = L.TOG_ELEM_WHITE
+        L.check(L.lib().tog_set_fixed_elements(solver.handle, state.ctypes.data_as(L.C.c_void_p)))
+        self.solver = solver
+        return self
+
+    def detach(self):
+        """Make every cell of the attached solver free again."""
+        if self.solver is not None:
+            L.check(L.lib().tog_set_fixed_elements(self.solver.handle, None))
+            self.solver = None
+
+    def _handle(self):
+        if self.solver is None:
+            raise RuntimeError("FixedElementProjectorFun runs on the device: attach it to a GB300FEASolver "
+                               "(get_fixed_element_projector(solver, black_cells, white_cells)) first")
+        return self.solver.handle
+
+    def __call__(self, x_free):
+        h = self._handle()
+        x = np.ascontiguousarray(x_free.x if isinstance(x_free, PseudoDensities) else x_free, dtype=np.float64)
+        if x.ndim != 1:
+            raise ValueError("x_free must be a vector")
+        rho = np.empty(self.nel)
+        try:
+            L.check(L.lib().tog_fixed_element_project(h, L.dptr(x) if x.size else None, x.size, L.dptr(rho)))
+        except L.TopOptError as e:
+            if e.code == L.TOG_ERR_ARG:
+                raise ValueError(str(e)) from None   # ArgumentError in the reference
+            raise
+        return rho
+
+    def pullback(self, drho):
+        h = self._handle()
+        d = np.ascontiguousarray(drho, dtype=np.float64)
+        if d.shape != (self.nel,):
+            raise ValueError("DimensionMismatch: one cotangent per cell")
+        out = np.empty(get_free_variable_count(self))
+        L.check(L.lib().tog_fixed_element_pullback(h, L.dptr(d), L.dptr(out) if out.size else None))
+        return out
+
+
+def get_free_variables(p):
+    """The free-cell mask (fixed_element.jl:88)."""
+    return p.free
+
+
+def get_free_variable_count(p):
+    """count(free) (fixed_element.jl:95)."""
+    return int(np.count_nonzero(p.free))
+
+
+def get_fixed_element_projector(target, black_cells, white_cells):
+    """get_fixed_element_projector(problem | nel, black_cells, white_cells)
+    (fixed_element.jl:127-159) with 0-based cell indices (the reference's are 1-based).
+    Given a GB300FEASolver it also attaches the projector to it."""
+    if isinstance(target, GB300FEASolver):
+        nel = target.problem.ncells
+    elif hasattr(target, "ncells"):
+        nel = target.ncells
+    else:
+        nel = int(target)
+    black = np.zeros(nel, dtype=bool)
+    white = np.zeros(nel, dtype=bool)
+    black[np.asarray(black_cells, dtype=np.int64)] = True
+    white[np.asarray(white_cells, dtype=np.int64)] = True
+    p = FixedElementProjectorFun(nel, black, white)
+    if isinstance(target, GB300FEASolver):
+        p.attach(target)
+    return p
+
+
 def oc_update(solver, x, dc, dv, vol_weights, volfrac, move=0.2):
     """Optimality-criteria update (published method; no reference counterpart).
     Returns (x_new, change, lambda)."""
