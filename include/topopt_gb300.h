@@ -49,6 +49,7 @@ enum tog_warm_start { TOG_WARM_COLD = 0, TOG_WARM_PREVIOUS = 1, TOG_WARM_LEARNED
 enum tog_filter_op { TOG_FILTER_J = 0, TOG_FILTER_JT = 1 };
 enum tog_projection_kind { TOG_PROJ_HEAVISIDE = 1, TOG_PROJ_SIGMOID = 2 };
 enum tog_element_state { TOG_ELEM_FREE = 0, TOG_ELEM_BLACK = 1, TOG_ELEM_WHITE = 2 };
+enum tog_optimizer { TOG_OPT_OC = 0, TOG_OPT_MMA = 1 };
 
 typedef struct tog_handle tog_handle;
 
@@ -175,10 +176,26 @@ int tog_fixed_element_pullback(tog_handle* h, const double* drho, double* dx_fre
 int tog_oc_update(tog_handle* h, const double* x, const double* dc, const double* dv, const double* vol_weights,
                   double volfrac, double move, double* x_new, double* change, double* lambda);
 
+/* ---- MMA, the method of moving asymptotes (Svanberg 1987), one inequality constraint ----
+ * The optimizer of TopOpt.jl's SIMP scripts (Nonconvex MMA87: docs/tutorials/simp.qmd:107-114,
+ * test/integration/test_end_to_end.jl:30-47), which is not part of TopOpt.jl: the published
+ * method with the asymptote, bound and coefficient rules of Svanberg's 2007 notes on
+ * x in [0, 1]^n, its dual solved by bisection on the multiplier.  The handle keeps the
+ * asymptotes and the last two iterates between calls (tog_mma_reset starts over).
+ * Minimises f subject to g(x) <= 0 given df0 = df/dx, g and dg = dg/dx at x; move is the
+ * move limit (0.5 in Svanberg's notes).  Cells fixed by tog_set_fixed_elements keep their
+ * densities.  Cell-sized host arrays. */
+int tog_mma_update(tog_handle* h, const double* x, const double* df0, double g, const double* dg, double move,
+                   double* x_new, double* change, double* lambda);
+int tog_mma_reset(tog_handle* h);
+
 /* ---- one SIMP design iteration, device-resident --------------------------------------
  * filter -> solve -> compliance/sensitivities -> filter pullback -> OC, the loop of
  * docs/tutorials/simp.qmd:86-114 with OC in place of MMA. */
 /* filter_kind: TOG_FILTER_NONE / DENSITY / SENS (needs rmin > 0). x0: initial design. */
+/* The optimizer of tog_simp_step: TOG_OPT_OC (default; tog_simp_init's move) or TOG_OPT_MMA
+ * (volume constraint sum(w x) <= volfrac; move <= 0 selects 0.5).  Restarts MMA's history. */
+int tog_simp_set_optimizer(tog_handle* h, int32_t optimizer, double move);
 int tog_simp_init(tog_handle* h, int32_t filter_kind, double rmin, double volfrac, double move, const double* x0);
 /* precision: TOG_FP64 (cold start, as the reference) or TOG_FP32_IR; warm_start: see
  * tog_warm_start (nonzero starts each solve from the previous displacement). */

@@ -626,6 +626,105 @@ def oc_update(x, dc, dv, vol_weights, volfrac, move=0.2, l1=0.0, l2=1e9, tol=1e-
     return xnew, change, lmid, steps
 
 
+class MMA:
+    """MMA, the method of moving asymptotes (Svanberg 1987), for min f s.t. g <= 0 on
+    x in [0, 1]^n: the optimizer of TopOpt.jl's SIMP scripts (Nonconvex MMA87,
+    docs/tutorials/simp.qmd:107-114, test/integration/test_end_to_end.jl:30-47).
+    Nonconvex is not part of TopOpt.jl (parity unpinned): this restates the published
+    method with the rules of Svanberg's 2007 notes on MMA -- asymptotes x -/+ 0.5 for the
+    first two iterations, then widened by 1.2 / narrowed by 0.7 as the last two steps
+    agree / oscillate, kept in [x - 10, x - 0.01] / [x + 0.01, x + 10]; bounds
+    alpha = max(L + 0.1 (x - L), x - move, 0), beta = min(U - 0.1 (U - x), x + move, 1);
+    p = (U - x)^2 (max(df, 0) + 1e-3 |df| + 1e-5), q = (x - L)^2 (max(-df, 0) + 1e-3 |df|
+    + 1e-5) -- and the subproblem solved through its dual in the single multiplier
+    lambda by bisection in log lambda on [1e-30, 1e30] (lambda = 0 when the approximated
+    constraint is inactive there)."""
+
+    def __init__(self, n, move=0.5, fixed=None):
+        self.n, self.move, self.fixed = n, move, fixed
+        self.k = 0
+        self.low = self.upp = self.x1 = self.x2 = None
+
+    @staticmethod
+    def _xlam(lam, p0, q0, p1, q1, L, U, a, b):
+        sp, sq = np.sqrt(p0 + lam * p1), np.sqrt(q0 + lam * q1)
+        return np.minimum(b, np.maximum(a, (L * sp + U * sq) / (sp + sq)))
+
+    def update(self, x, df0, g, dg):
+        """One MMA step from x with f's gradient df0, the constraint value g and its
+        gradient dg.  Returns (x_new, change, lambda, dual evaluations)."""
+        x = np.asarray(x, dtype=np.float64)
+        df0 = np.asarray(df0, dtype=np.float64)
+        dg = np.asarray(dg, dtype=np.float64)
+        self.k += 1
+        if self.k <= 2:
+            L, U = x - 0.5, x + 0.5
+        else:
+            zz = (x - self.x1) * (self.x1 - self.x2)
+            f = np.where(zz > 0, 1.2, np.where(zz < 0, 0.7, 1.0))
+            L = x - f * (self.x1 - self.low)
+            U = x + f * (self.upp - self.x1)
+            L = np.minimum(np.maximum(L, x - 10.0), x - 0.01)
+            U = np.minimum(np.maximum(U, x + 0.01), x + 10.0)
+        a = np.maximum(np.maximum(L + 0.1 * (x - L), x - self.move), 0.0)
+        b = np.minimum(np.minimum(U - 0.1 * (U - x), x + self.move), 1.0)
+        if self.fixed is not None:
+            a[self.fixed.black] = b[self.fixed.black] = 1.0
+            a[self.fixed.white] = b[self.fixed.white] = 0.0
+        ux2, xl2 = (U - x) ** 2, (x - L) ** 2
+        r0, r1 = 1e-3 * np.abs(df0) + 1e-5, 1e-3 * np.abs(dg) + 1e-5
+        p0, q0 = (np.maximum(df0, 0) + r0) * ux2, (np.maximum(-df0, 0) + r0) * xl2
+        p1, q1 = (np.maximum(dg, 0) + r1) * ux2, (np.maximum(-dg, 0) + r1) * xl2
+        r = float(np.sum(p1 / (U - x) + q1 / (x - L))) - g
+
+        def h(lam):
+            xe = self._xlam(lam, p0, q0, p1, q1, L, U, a, b)
+            return float(np.sum(p1 / (U - xe) + q1 / (xe - L))) - r
+
+        steps = 1
+        if h(0.0) <= 0.0:
+            lam = 0.0
+        else:
+            lo, hi = math.log(1e-30), math.log(1e30)
+            while True:
+                mid = 0.5 * (lo + hi)
+                if h(math.exp(mid)) > 0.0:
+                    lo = mid
+                else:
+                    hi = mid
+                steps += 1
+                if hi - lo <= 1e-12 or steps >= 72:
+                    break
+            lam = math.exp(0.5 * (lo + hi))
+        xn = self._xlam(lam, p0, q0, p1, q1, L, U, a, b)
+        self.low, self.upp = L, U
+        self.x2, self.x1 = self.x1, x.copy()
+        return xn, float(np.max(np.abs(xn - x))), lam, steps
+
+
+def simp_iteration_mma(st: FEAState, x, filt, volfrac, mma: MMA, solve="direct", rtol=1e-10, maxiter=100000):
+    """One design iteration with MMA in place of OC: the volume constraint
+    g = sum(w x) - volfrac, w = J'(1/n) (the filtered volume fraction) with the density
+    filter, 1/n otherwise (docs/tutorials/simp.qmd:86-114)."""
+    xf = filt.forward(x) if filt is not None else x.copy()
+    st.vars = xf
+    if solve == "direct":
+        u, its = direct_solve(st), 0
+    else:
+        u, its, _ = pcg(st, rtol=rtol, maxiter=maxiter)
+    c, gr, _ = compliance(st, u, xf)
+    n = st.prob.grid.ncells
+    dv = np.full(n, 1.0 / n)
+    if filt is not None:
+        dc = filt.pullback(gr)
+        dv = filt.pullback(dv) if isinstance(filt, DensityFilter) else dv
+    else:
+        dc = gr
+    g = float(np.dot(dv, x)) - volfrac
+    xnew, change, lam, steps = mma.update(x, dc, g, dv)
+    return dict(x_new=xnew, xf=xf, u=u, c=c, dc=dc, dv=dv, change=change, lam=lam, steps=steps, cg_iters=its)
+
+
 def simp_iteration(st: FEAState, x, filt, volfrac, move=0.2, solve="direct",
                    rtol=1e-10, maxiter=100000, vol_weights=None, fixed=None):
     """One design iteration: filter -> solve -> compliance/sens -> filter pullback

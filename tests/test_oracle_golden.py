@@ -235,3 +235,27 @@ def test_oc_holds_fixed_cells(O):
     B = x * np.sqrt(-dc / w)
     free = np.clip(B / np.sqrt(lam), np.maximum(0, x - 0.2), np.minimum(1, x + 0.2))
     assert np.array_equal(xn[fx.free], free[fx.free])
+
+
+# ---------------------------------------------------------------- MMA (Nonconvex MMA87's method)
+def test_mma_reaches_the_analytic_optimum(O):
+    """MMA on min sum(c_j / x_j) s.t. mean(x) <= V over [0, 1]^n, whose optimum is
+    x_j = V n sqrt(c_j) / sum(sqrt(c)) (inside the bounds here): the restated method
+    converges to it, and an inactive constraint gives lambda = 0."""
+    rng = np.random.default_rng(3)
+    n, V = 50, 0.4
+    c = rng.uniform(0.5, 1.5, n)
+    xs = V * n * np.sqrt(c) / np.sum(np.sqrt(c))
+    assert xs.max() < 1.0
+    m = O.MMA(n)
+    x = np.full(n, V)
+    for _ in range(60):
+        x, ch, lam, _ = m.update(x, -c / x ** 2, float(np.mean(x)) - V, np.full(n, 1.0 / n))
+    assert np.max(np.abs(x - xs)) < 1e-6
+    assert lam > 0
+    # an objective that lowers x leaves the constraint inactive: lambda = 0 after one
+    # dual evaluation, and x moves down to its lower bound max(L + 0.1 (x - L), x - move, 0)
+    m2 = O.MMA(n)
+    x2, _, lam2, steps = m2.update(np.full(n, 0.5), c, 0.5 - 0.9, np.full(n, 1.0 / n))
+    assert lam2 == 0.0 and steps == 1
+    assert np.all(x2 < 0.5)

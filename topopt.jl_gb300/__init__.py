@@ -35,5 +35,7 @@ from .topopt_api import (  # noqa: F401
     get_free_variables,
     grid_counts,
     node_dofs,
+    mma_reset,
+    mma_update,
     oc_update,
 )

@@ -13,6 +13,7 @@ TOG_OK, TOG_ERR_ARG, TOG_ERR_CUDA, TOG_NOT_CONVERGED, TOG_BREAKDOWN, TOG_ERR_STA
 TOG_FP64, TOG_FP32_IR = 0, 1
 TOG_PROJ_HEAVISIDE, TOG_PROJ_SIGMOID = 1, 2
 TOG_ELEM_FREE, TOG_ELEM_BLACK, TOG_ELEM_WHITE = 0, 1, 2
+TOG_OPT_OC, TOG_OPT_MMA = 0, 1
 TOG_FILTER_NONE, TOG_FILTER_DENSITY, TOG_FILTER_SENS = 0, 1, 2
 TOG_FILTER_J, TOG_FILTER_JT = 0, 1
 
@@ -104,6 +105,9 @@ SIGNATURES = {
     "tog_free_variable_count": (C.c_int, [_H, _I64]),
     "tog_fixed_element_project": (C.c_int, [_H, _D, C.c_int64, _D]),
     "tog_fixed_element_pullback": (C.c_int, [_H, _D, _D]),
+    "tog_mma_update": (C.c_int, [_H, _D, _D, C.c_double, _D, C.c_double, _D, _D, _D]),
+    "tog_mma_reset": (C.c_int, [_H]),
+    "tog_simp_set_optimizer": (C.c_int, [_H, C.c_int32, C.c_double]),
     "tog_oc_update_noalloc": (C.c_int, [C.c_int64, _D, _D, _D, _D, C.c_double, C.c_double, _D, _D, C.c_void_p]),
 }
 

@@ -18,6 +18,7 @@
 #include "tog_mv3.cuh"
 #include "tog_mv3x2.cuh"
 #include "tog_march3.cuh"
+#include "tog_mma.cuh"
 
 using namespace tog;
 
@@ -121,6 +122,14 @@ struct tog_handle {
     // -1 black, -2 white; null when every cell is free
     int* d_fpos = nullptr;
     long long nfree = 0;
+    // MMA: state, asymptotes / history / coefficients (10 cell vectors), iteration count
+    MmaState* d_mma = nullptr;
+    MmaState* h_mma = nullptr;
+    double* d_mma_buf = nullptr;
+    int mma_k = 0;
+    int simp_opt = TOG_OPT_OC;
+    double mma_move = 0.5;
+    cudaGraphExec_t g_mma = nullptr;
     // learned warm start (3D): network, previous-iteration state and recording hook
     tog_nn* net = nullptr;
     double* d_vars_prev = nullptr;   // physical densities of the previous design iteration
@@ -872,6 +881,68 @@ int oc_dev(tog_handle* h, double volfrac, double move) {
     return TOG_OK;
 }
 
+MmaArgs mma_args(tog_handle* h, const double* w) {
+    MmaArgs A{};
+    const long long n = h->ncells;
+    A.x = h->d_x;
+    A.df0 = h->d_dc;
+    A.dg = h->d_dv;
+    A.w = w;
+    A.fpos = h->d_fpos;
+    double* b = h->d_mma_buf;
+    A.low = b;
+    A.upp = b + n;
+    A.xold1 = b + 2 * n;
+    A.xold2 = b + 3 * n;
+    A.alfa = b + 4 * n;
+    A.beta = b + 5 * n;
+    A.p0 = b + 6 * n;
+    A.q0 = b + 7 * n;
+    A.p1 = b + 8 * n;
+    A.q1 = b + 9 * n;
+    A.xnew = h->d_xnew;
+    A.n = n;
+    A.st = h->d_mma;
+    A.partials = h->d_partials;
+    return A;
+}
+
+int mma_buffers(tog_handle* h) {
+    if (h->d_mma) return TOG_OK;
+    TOG_TRY(dalloc(&h->d_mma, 1));
+    TOG_TRY(dalloc(&h->d_mma_buf, 10 * (size_t)h->ncells));
+    TOG_CUDA(cudaMallocHost(&h->h_mma, sizeof(MmaState)));
+    TOG_CUDA(cudaMemsetAsync(h->d_mma, 0, sizeof(MmaState), h->stream));
+    return TOG_OK;
+}
+
+// One MMA update on the device arrays d_x, d_dc (objective gradient), d_dv (constraint
+// gradient) -> d_xnew.  With use_w the constraint is sum(d_w x) - volfrac, else g.
+int mma_dev(tog_handle* h, bool use_w, double g, double volfrac, double move) {
+    TOG_TRY(mma_buffers(h));
+    const int nb = h->ew_blocks(h->ncells);
+    if (!h->g_mma) {
+        cudaGraph_t gr = nullptr;
+        const MmaArgs A = mma_args(h, h->d_w);
+        TOG_CUDA(cudaStreamBeginCapture(h->own, cudaStreamCaptureModeThreadLocal));
+        for (int i = 0; i < kMmaMaxSteps; ++i) k_mma_step<<<nb, kEwThreads, 0, h->own>>>(A);
+        k_mma_final<<<nb, kEwThreads, 0, h->own>>>(A);
+        TOG_CUDA(cudaStreamEndCapture(h->own, &gr));
+        TOG_CUDA(cudaGraphInstantiate(&h->g_mma, gr, 0));
+        cudaGraphDestroy(gr);
+    }
+    h->mma_k += 1;
+    k_mma_prep<<<nb, kEwThreads, 0, h->stream>>>(mma_args(h, use_w ? h->d_w : nullptr), h->mma_k, g, volfrac,
+                                                 move);
+    TOG_LAUNCHED(1);
+    TOG_CUDA(cudaGetLastError());
+    TOG_CUDA(cudaGraphLaunch(h->g_mma, h->stream));
+    TOG_LAUNCHED(kMmaMaxSteps + 1);
+    TOG_CUDA(cudaMemcpyAsync(h->h_mma, h->d_mma, sizeof(MmaState), cudaMemcpyDeviceToHost, h->stream));
+    TOG_CUDA(cudaStreamSynchronize(h->stream));
+    return TOG_OK;
+}
+
 int upload_dofs(tog_handle* h, const double* ref, double* d_internal) {
     TOG_CUDA(cudaMemcpyAsync(h->d_tmp2, ref, h->ndofs * sizeof(double), cudaMemcpyHostToDevice, h->stream));
     k_gather_d<<<h->ew_blocks(h->ndofs), kEwThreads, 0, h->stream>>>(h->d_tmp2, h->d_int2ref, d_internal, h->ndofs);
@@ -1183,11 +1254,13 @@ int tog_destroy(tog_handle* h) {
     if (h->g_pcg64) cudaGraphExecDestroy(h->g_pcg64);
     if (h->g_pcg32) cudaGraphExecDestroy(h->g_pcg32);
     if (h->g_oc) cudaGraphExecDestroy(h->g_oc);
+    if (h->g_mma) cudaGraphExecDestroy(h->g_mma);
+    if (h->h_mma) cudaFreeHost(h->h_mma);
     void* ptrs[] = {h->d_int2ref, h->d_ref2int, h->d_fixmask, h->d_vecpool, h->d_vars,    h->d_e64,
                     h->d_e32,     h->d_dinv64,  h->d_dinv32,  h->d_nodal,   h->d_st64,    h->d_st32,
                     h->d_oc,      h->d_partials, h->d_cnt,    h->d_scalar,  h->d_invW,    h->d_soff,
                     h->d_sw,      h->d_vars_prev, h->d_uprev, h->d_du_last, h->d_nn_in, h->d_nn_out, h->d_nn_sc,
-                    h->d_nn_part, h->d_nn_cnt, h->d_fpos};
+                    h->d_nn_part, h->d_nn_cnt, h->d_fpos, h->d_mma, h->d_mma_buf};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (int i = 0; i < 6; ++i)
@@ -1397,10 +1470,12 @@ int tog_set_fixed_elements(tog_handle* h, const uint8_t* state) {
         h->nfree = nf;
     }
     // the OC graph holds the mask pointer: capture it again on the next update
-    if (h->g_oc) {
+    if (h->g_oc || h->g_mma) {
         TOG_CUDA(cudaStreamSynchronize(h->stream));
-        cudaGraphExecDestroy(h->g_oc);
+        if (h->g_oc) cudaGraphExecDestroy(h->g_oc);
+        if (h->g_mma) cudaGraphExecDestroy(h->g_mma);
         h->g_oc = nullptr;
+        h->g_mma = nullptr;
     }
     if (h->d_fpos && h->simp_ready) {   // an active loop's design follows the new mask at once
         k_fixed_pin<<<h->ew_blocks(h->ncells), kEwThreads, 0, h->stream>>>(h->d_x, h->d_fpos, h->ncells);
@@ -1478,6 +1553,42 @@ int tog_oc_update(tog_handle* h, const double* x, const double* dc, const double
     return TOG_OK;
 }
 
+int tog_mma_update(tog_handle* h, const double* x, const double* df0, double g, const double* dg, double move,
+                   double* x_new, double* change, double* lambda) {
+    TOG_TRY(check_handle(h));
+    if (!x || !df0 || !dg || !x_new) return fail(TOG_ERR_ARG, "null array");
+    if (!(move > 0 && move <= 1) || !std::isfinite(g)) return fail(TOG_ERR_ARG, "need 0 < move <= 1 and a finite g");
+    if (h->simp_ready) return fail(TOG_ERR_STATE, "tog_mma_update shares buffers with an active tog_simp loop");
+    const size_t bytes = h->ncells * sizeof(double);
+    TOG_CUDA(cudaMemcpyAsync(h->d_x, x, bytes, cudaMemcpyHostToDevice, h->stream));
+    TOG_CUDA(cudaMemcpyAsync(h->d_dc, df0, bytes, cudaMemcpyHostToDevice, h->stream));
+    TOG_CUDA(cudaMemcpyAsync(h->d_dv, dg, bytes, cudaMemcpyHostToDevice, h->stream));
+    TOG_TRY(mma_dev(h, false, g, 0.0, move));
+    TOG_CUDA(cudaMemcpyAsync(x_new, h->d_xnew, bytes, cudaMemcpyDeviceToHost, h->stream));
+    TOG_CUDA(cudaStreamSynchronize(h->stream));
+    if (change) *change = h->h_mma->change;
+    if (lambda) *lambda = h->h_mma->lam;
+    return TOG_OK;
+}
+
+int tog_mma_reset(tog_handle* h) {
+    TOG_TRY(check_handle(h));
+    h->mma_k = 0;
+    return TOG_OK;
+}
+
+int tog_simp_set_optimizer(tog_handle* h, int32_t optimizer, double move) {
+    TOG_TRY(check_handle(h));
+    if (optimizer != TOG_OPT_OC && optimizer != TOG_OPT_MMA) return fail(TOG_ERR_ARG, "unknown optimizer");
+    if (optimizer == TOG_OPT_MMA) {
+        if (!(move <= 1)) return fail(TOG_ERR_ARG, "need move <= 1 (<= 0: the default 0.5)");
+        h->mma_move = move > 0 ? move : 0.5;
+    }
+    h->simp_opt = optimizer;
+    h->mma_k = 0;
+    return TOG_OK;
+}
+
 int tog_simp_init(tog_handle* h, int32_t filter_kind, double rmin, double volfrac, double move, const double* x0) {
     TOG_TRY(check_handle(h));
     if (!x0) return fail(TOG_ERR_ARG, "null x0");
@@ -1507,6 +1618,7 @@ int tog_simp_init(tog_handle* h, int32_t filter_kind, double rmin, double volfra
     TOG_CUDA(cudaStreamSynchronize(h->stream));
     h->simp_ready = true;
     h->u_valid = false;
+    h->mma_k = 0;
     return TOG_OK;
 }
 
@@ -1554,19 +1666,23 @@ int tog_simp_step(tog_handle* h, int32_t precision, double rtol, int32_t maxiter
         TOG_TRY(filter_dev(h, TOG_FILTER_J, h->d_grad, h->d_dc));
     else
         TOG_CUDA(cudaMemcpyAsync(h->d_dc, h->d_grad, bytes, cudaMemcpyDeviceToDevice, h->stream));
-    TOG_TRY(oc_dev(h, h->volfrac, h->move));
+    if (h->simp_opt == TOG_OPT_MMA)
+        TOG_TRY(mma_dev(h, true, 0.0, h->volfrac, h->mma_move));
+    else
+        TOG_TRY(oc_dev(h, h->volfrac, h->move));
     TOG_CUDA(cudaMemcpyAsync(h->h_scalar, h->d_scalar, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     TOG_CUDA(cudaStreamSynchronize(h->stream));
     TOG_CUDA(cudaMemcpyAsync(h->d_x, h->d_xnew, bytes, cudaMemcpyDeviceToDevice, h->stream));
     TOG_CUDA(cudaStreamSynchronize(h->stream));
     if (stats) {
+        const bool mma = h->simp_opt == TOG_OPT_MMA;
         stats->compliance = h->h_scalar[0];
-        stats->volume = h->h_oc->vol;
-        stats->change = h->h_oc->change;
-        stats->lambda = h->h_oc->lmid;
+        stats->volume = mma ? h->h_mma->vol : h->h_oc->vol;
+        stats->change = mma ? h->h_mma->change : h->h_oc->change;
+        stats->lambda = mma ? h->h_mma->lam : h->h_oc->lmid;
         stats->cg_iterations = ss.iterations;
         stats->outer_iterations = ss.outer_iterations;
-        stats->oc_steps = h->h_oc->steps;
+        stats->oc_steps = mma ? h->h_mma->steps : h->h_oc->steps;
         stats->status = ss.status;
         stats->rel_residual = ss.rel_residual;
     }

@@ -33,7 +33,7 @@ using Ferrite
 
 export GB300Solver, GB300FEASolver, GB300DensityFilter, GB300SensFilter, oc_update!, simp_step!
 export BatchedSIMP, batch_step!, batch_results, WarmStartNet, attach_network!
-export GB300FixedElementProjector, clear_fixed_elements!, GB300ProjectedDensityFilter
+export GB300FixedElementProjector, clear_fixed_elements!, GB300ProjectedDensityFilter, mma_update!, mma_reset!
 
 const libtog = joinpath(@__DIR__, "..", "libtopopt_gb300.so")
 
@@ -317,6 +317,25 @@ function ChainRulesCore.rrule(g::GB300FixedElementProjector, x_free::AbstractVec
     end
 end
 
+"""
+    mma_update!(xnew, solver, x, df0, g, dg; move=0.5) -> (change, λ)
+    mma_reset!(solver)
+
+One step of MMA (Svanberg's method of moving asymptotes, what `optimize(model, MMA87(), x0)`
+runs in the reference's SIMP scripts) on the GPU for min f s.t. g(x) <= 0 on [0, 1]^n.
+The asymptotes and the last two iterates stay in the solver's handle between calls.
+"""
+function mma_update!(xnew::Vector{Float64}, s::GB300FEASolver, x, df0, g::Real, dg; move=0.5)
+    ch, lam = Ref(0.0), Ref(0.0)
+    check(ccall((:tog_mma_update, libtog), Cint,
+                (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Float64, Ptr{Float64}, Float64, Ptr{Float64},
+                 Ref{Float64}, Ref{Float64}),
+                s.handle, Vector{Float64}(x), Vector{Float64}(df0), Float64(g), Vector{Float64}(dg), Float64(move),
+                xnew, ch, lam))
+    return ch[], lam[]
+end
+mma_reset!(s::GB300FEASolver) = check(ccall((:tog_mma_reset, libtog), Cint, (Ptr{Cvoid},), s.handle))
+
 mutable struct IterStats
     compliance::Float64
     volume::Float64
@@ -336,10 +355,15 @@ IterStats() = IterStats(0, 0, 0, 0, 0, 0, 0, 0, 0)
 
 Device-resident SIMP loop: one call per design iteration, the design stays in HBM.
 """
-function simp_init!(s::GB300FEASolver, x0::AbstractVector; volfrac, rmin=0.0, filter=:density, move=0.2)
+function simp_init!(s::GB300FEASolver, x0::AbstractVector; volfrac, rmin=0.0, filter=:density, move=nothing,
+                    optimizer=:oc)
     kind = filter === :density ? Int32(1) : filter === :sens ? Int32(2) : Int32(0)
+    opt = optimizer === :mma ? Int32(1) : Int32(0)
+    check(ccall((:tog_simp_set_optimizer, libtog), Cint, (Ptr{Cvoid}, Int32, Float64), s.handle, opt,
+                optimizer === :mma && move !== nothing ? Float64(move) : 0.0))
+    ocmove = optimizer === :oc && move !== nothing ? Float64(move) : 0.2
     check(ccall((:tog_simp_init, libtog), Cint, (Ptr{Cvoid}, Int32, Float64, Float64, Float64, Ptr{Float64}),
-                s.handle, kind, Float64(rmin), Float64(volfrac), Float64(move), Vector{Float64}(x0)))
+                s.handle, kind, Float64(rmin), Float64(volfrac), ocmove, Vector{Float64}(x0)))
 end
 function simp_step!(s::GB300FEASolver)
     st = Ref(IterStats())

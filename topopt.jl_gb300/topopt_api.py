@@ -543,17 +543,46 @@ def oc_update(solver, x, dc, dv, vol_weights, volfrac, move=0.2):
     return xn, ch.value, lam.value
 
 
+def mma_update(solver, x, df0, g, dg, move=0.5):
+    """One MMA step on the device (Svanberg's method of moving asymptotes, the optimizer
+    of the reference's SIMP scripts through Nonconvex MMA87; see include/topopt_gb300.h):
+    min f s.t. g(x) <= 0 on [0, 1]^n, with the asymptotes and the last two iterates kept
+    in the solver's handle between calls (mma_reset(solver) starts over).
+    Returns (x_new, change, lambda)."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    df0 = np.ascontiguousarray(df0, dtype=np.float64)
+    dg = np.ascontiguousarray(dg, dtype=np.float64)
+    xn = np.empty_like(x)
+    ch, lam = L.C.c_double(), L.C.c_double()
+    L.check(L.lib().tog_mma_update(solver.handle, L.dptr(x), L.dptr(df0), float(g), L.dptr(dg), float(move),
+                                   L.dptr(xn), L.C.byref(ch), L.C.byref(lam)))
+    return xn, ch.value, lam.value
+
+
+def mma_reset(solver):
+    L.check(L.lib().tog_mma_reset(solver.handle))
+
+
 class SIMPLoop:
     """Device-resident SIMP design loop: filter -> solve -> compliance/sensitivities
     -> filter pullback -> OC, one C-ABI call per design iteration."""
 
     FILTERS = {"none": L.TOG_FILTER_NONE, "density": L.TOG_FILTER_DENSITY, "sens": L.TOG_FILTER_SENS}
 
-    def __init__(self, solver, *, volfrac, rmin=0.0, filter="density", move=0.2, x0=None):
+    OPTIMIZERS = {"oc": L.TOG_OPT_OC, "mma": L.TOG_OPT_MMA}
+
+    def __init__(self, solver, *, volfrac, rmin=0.0, filter="density", move=None, x0=None, optimizer="oc"):
+        """optimizer "oc" (move default 0.2) or "mma" (the volume constraint through MMA,
+        move default 0.5)."""
         self.solver = solver
         n = solver.problem.ncells
+        if optimizer not in self.OPTIMIZERS:
+            raise ValueError("optimizer must be one of %s" % sorted(self.OPTIMIZERS))
         x0 = np.full(n, float(volfrac)) if x0 is None else np.ascontiguousarray(x0, dtype=np.float64)
-        L.check(L.lib().tog_simp_init(solver.handle, self.FILTERS[filter], float(rmin), float(volfrac), float(move),
+        oc_move = 0.2 if (move is None or optimizer != "oc") else float(move)
+        L.check(L.lib().tog_simp_set_optimizer(solver.handle, self.OPTIMIZERS[optimizer],
+                                               0.0 if (move is None or optimizer != "mma") else float(move)))
+        L.check(L.lib().tog_simp_init(solver.handle, self.FILTERS[filter], float(rmin), float(volfrac), oc_move,
                                       L.dptr(x0)))
 
     def step(self, precision=None, rtol=None, maxiter=None, warm_start=None):
