@@ -176,6 +176,22 @@ int tog_fixed_element_pullback(tog_handle* h, const double* drho, double* dx_fre
 int tog_oc_update(tog_handle* h, const double* x, const double* dc, const double* dv, const double* vol_weights,
                   double volfrac, double move, double* x_new, double* change, double* lambda);
 
+/* ---- multi-load compliance: MultiLoad (src/TopOptProblems/multiload.jl:21-46) with
+ *      MeanComplianceFun / BlockComplianceFun (src/Functions/mean_compliance.jl:8-150,
+ *      block_compliance.jl:7-110) ----
+ * The rhs columns F (CSC: colptr[ncol + 1], 0-based reference dof rows, values) are solved
+ * one after the other from zero (solvers_api.jl:293-348), prescribed dofs zeroed
+ * (apply_zero!), at the current vars; c[i] = f_i' u_i.  The cell gradient of every column
+ * stays on the device for tog_multiload_gradient.  Precision and tolerances as tog_solve.
+ * The handle's own rhs is kept; its displacement is that of the last column.  stats sums
+ * the PCG iterations of all columns; TOG_NOT_CONVERGED when a column missed the tolerance. */
+int tog_multiload_compliance(tog_handle* h, int32_t ncol, const int64_t* colptr, const int32_t* rowval,
+                             const double* nzval, int32_t precision, double rtol, double abstol, int32_t maxiter,
+                             double* c, tog_solve_stats* stats);
+/* out = sum_i w[i] dc_i/dx over the columns of the last tog_multiload_compliance: the mean
+ * compliance's gradient with w = 1/n, BlockComplianceFun's pullback with w = delta. */
+int tog_multiload_gradient(tog_handle* h, int32_t ncol, const double* w, double* out);
+
 /* ---- MMA, the method of moving asymptotes (Svanberg 1987), one inequality constraint ----
  * The optimizer of TopOpt.jl's SIMP scripts (Nonconvex MMA87: docs/tutorials/simp.qmd:107-114,
  * test/integration/test_end_to_end.jl:30-47), which is not part of TopOpt.jl: the published

@@ -725,6 +725,40 @@ def simp_iteration_mma(st: FEAState, x, filt, volfrac, mma: MMA, solve="direct",
     return dict(x_new=xnew, xf=xf, u=u, c=c, dc=dc, dv=dv, change=change, lam=lam, steps=steps, cg_iters=its)
 
 
+def multiload_compliance(st: FEAState, F, x):
+    """Per-column compliance and cell gradient of a load matrix F (ndofs x n, reference
+    dof rows): every column solved directly with its prescribed dofs zeroed, as the
+    solver's matrix-rhs call (src/FEA/solvers_api.jl:293-348) followed by
+    compute_compliance (src/Functions/mean_compliance.jl:78-99).  Returns (c[n],
+    G[ncells, n])."""
+    st.vars = np.asarray(x, dtype=np.float64)
+    F = sp.csc_matrix(F)
+    c = np.empty(F.shape[1])
+    G = np.empty((st.prob.grid.ncells, F.shape[1]))
+    for i in range(F.shape[1]):
+        u = direct_solve(st, np.asarray(F[:, i].toarray()).ravel())
+        c[i], G[:, i], _ = compliance(st, u, st.vars)
+    return c, G
+
+
+def mean_compliance(st: FEAState, F, x, method="exact"):
+    """MeanComplianceFun (mean_compliance.jl:8-150) with method exact (mean over F's
+    columns) or exact_svd (the columns U S of the thin SVD of F's nonzero rows, singular
+    values > 1e-6, src/Functions/trace.jl:15-34, divided by F's column count).
+    Returns (mean, gradient)."""
+    F = sp.csc_matrix(F)
+    n = F.shape[1]
+    if method == "exact_svd":
+        rows = np.unique(F.indices)
+        U, S, _ = np.linalg.svd(F[rows, :].toarray(), full_matrices=False)
+        keep = S > 1e-6
+        US = np.zeros((F.shape[0], int(keep.sum())))
+        US[rows, :] = U[:, keep] * S[keep]
+        F = sp.csc_matrix(US)
+    c, G = multiload_compliance(st, F, x)
+    return float(c.sum() / n), G.sum(axis=1) / n
+
+
 def simp_iteration(st: FEAState, x, filt, volfrac, move=0.2, solve="direct",
                    rtol=1e-10, maxiter=100000, vol_weights=None, fixed=None):
     """One design iteration: filter -> solve -> compliance/sens -> filter pullback

@@ -259,3 +259,26 @@ def test_mma_reaches_the_analytic_optimum(O):
     x2, _, lam2, steps = m2.update(np.full(n, 0.5), c, 0.5 - 0.9, np.full(n, 1.0 / n))
     assert lam2 == 0.0 and steps == 1
     assert np.all(x2 < 0.5)
+
+
+# ---------------------------------------------------------------- MultiLoad / MeanComplianceFun
+def test_mean_compliance_svd_equals_exact_and_fd(O):
+    """The SVD form of the mean compliance equals the column mean (tr(F' K^-1 F) / n is
+    invariant under F -> U S), and the gradient matches finite differences."""
+    prob = O.point_load_cantilever((8, 4), (1.0, 1.0))
+    st = O.fea_setup(prob, xmin=1e-3, p=3.0)
+    rng = np.random.default_rng(5)
+    F = np.zeros((prob.ndofs, 5))
+    dofs = rng.choice(np.arange(prob.ndofs), 3, replace=False)
+    F[dofs, :] = rng.standard_normal((3, 5))
+    x = rng.uniform(0.3, 0.9, prob.grid.ncells)
+    m1, g1 = O.mean_compliance(st, F, x, "exact")
+    m2, g2 = O.mean_compliance(st, F, x, "exact_svd")
+    assert abs(m1 - m2) / m1 < 1e-12
+    assert np.max(np.abs(g1 - g2)) / np.max(np.abs(g1)) < 1e-10
+    h = 1e-6
+    for e in (0, 7, 19):
+        xp = x.copy()
+        xp[e] += h
+        fd = (O.mean_compliance(st, F, xp, "exact")[0] - m1) / h
+        assert abs(fd - g1[e]) < 1e-4 * max(1.0, abs(g1[e]))

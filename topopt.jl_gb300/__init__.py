@@ -9,6 +9,7 @@ __graft_entry__.py; the directory name carries a dot).
 from ._lib import TopOptError, NotConverged, lib  # noqa: F401
 from .topopt_api import (  # noqa: F401
     BatchedSIMP,
+    BlockComplianceFun,
     ComplianceFun,
     DensityFilterFun,
     FEASolver,
@@ -18,6 +19,8 @@ from .topopt_api import (  # noqa: F401
     HalfMBB,
     HeavisideProjectionFun,
     LoadedCantilever,
+    MeanComplianceFun,
+    MultiLoad,
     PointLoadCantilever,
     PowerPenaltyFun,
     ProjectedDensityFilterFun,
@@ -30,6 +33,10 @@ from .topopt_api import (  # noqa: F401
     cell_dofs,
     config3_problems,
     element_stiffness,
+    find_nearest_dofs,
+    generate_scenarios,
+    hadamard,
+    hutch_rand,
     get_fixed_element_projector,
     get_free_variable_count,
     get_free_variables,

@@ -107,6 +107,9 @@ SIGNATURES = {
     "tog_fixed_element_pullback": (C.c_int, [_H, _D, _D]),
     "tog_mma_update": (C.c_int, [_H, _D, _D, C.c_double, _D, C.c_double, _D, _D, _D]),
     "tog_mma_reset": (C.c_int, [_H]),
+    "tog_multiload_compliance": (C.c_int, [_H, C.c_int32, _I64, _I32, _D, C.c_int32, C.c_double, C.c_double,
+                                           C.c_int32, _D, C.c_void_p]),
+    "tog_multiload_gradient": (C.c_int, [_H, C.c_int32, _D, _D]),
     "tog_simp_set_optimizer": (C.c_int, [_H, C.c_int32, C.c_double]),
     "tog_oc_update_noalloc": (C.c_int, [C.c_int64, _D, _D, _D, _D, C.c_double, C.c_double, _D, _D, C.c_void_p]),
 }

@@ -123,6 +123,10 @@ struct tog_handle {
     int* d_fpos = nullptr;
     long long nfree = 0;
     // MMA: state, asymptotes / history / coefficients (10 cell vectors), iteration count
+    // multi-load compliance: per-column cell gradients, saved single-load rhs, host maps
+    double* d_mlg = nullptr;
+    long long mlg_cols = 0;
+    double* d_fsave = nullptr;
     MmaState* d_mma = nullptr;
     MmaState* h_mma = nullptr;
     double* d_mma_buf = nullptr;
@@ -1260,7 +1264,7 @@ int tog_destroy(tog_handle* h) {
                     h->d_e32,     h->d_dinv64,  h->d_dinv32,  h->d_nodal,   h->d_st64,    h->d_st32,
                     h->d_oc,      h->d_partials, h->d_cnt,    h->d_scalar,  h->d_invW,    h->d_soff,
                     h->d_sw,      h->d_vars_prev, h->d_uprev, h->d_du_last, h->d_nn_in, h->d_nn_out, h->d_nn_sc,
-                    h->d_nn_part, h->d_nn_cnt, h->d_fpos, h->d_mma, h->d_mma_buf};
+                    h->d_nn_part, h->d_nn_cnt, h->d_fpos, h->d_mma, h->d_mma_buf, h->d_mlg, h->d_fsave};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (int i = 0; i < 6; ++i)
@@ -1369,6 +1373,146 @@ int tog_set_u(tog_handle* h, const double* u) {
     TOG_TRY(upload_dofs(h, u, h->d_u));
     TOG_CUDA(cudaStreamSynchronize(h->stream));
     h->u_valid = true;
+    return TOG_OK;
+}
+
+// rhs column scatter: f[idx[k]] = val[k] (f zeroed before; prescribed dofs already dropped)
+__global__ void k_scatter_pairs(double* __restrict__ f, const long long* __restrict__ idx,
+                                const double* __restrict__ val, int n) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) f[idx[k]] = val[k];
+}
+// out = sum_i w_i g_i over the per-column cell gradients (column-major ncells x ncol)
+__global__ void __launch_bounds__(256) k_weighted_cols(const double* __restrict__ g, const double* __restrict__ w,
+                                                       int ncol, long long ncells, double* __restrict__ out) {
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < ncells;
+         e += (long long)gridDim.x * blockDim.x) {
+        double acc = 0.0;
+        for (int i = 0; i < ncol; ++i) acc = fma(w[i], g[(size_t)i * ncells + e], acc);
+        out[e] = acc;
+    }
+}
+
+int tog_multiload_compliance(tog_handle* h, int32_t ncol, const int64_t* colptr, const int32_t* rowval,
+                             const double* nzval, int32_t precision, double rtol, double abstol, int32_t maxiter,
+                             double* c, tog_solve_stats* stats) {
+    TOG_TRY(check_handle(h));
+    if (ncol <= 0 || !colptr || !c || (colptr[ncol] > 0 && (!rowval || !nzval)))
+        return fail(TOG_ERR_ARG, "need ncol > 0, colptr[ncol + 1], rowval, nzval and c[ncol]");
+    if (colptr[0] != 0) return fail(TOG_ERR_ARG, "colptr[0] must be 0");
+    for (int i = 0; i < ncol; ++i)
+        if (colptr[i + 1] < colptr[i]) return fail(TOG_ERR_ARG, "colptr must be non-decreasing");
+    for (long long k = 0; k < colptr[ncol]; ++k) {
+        if (rowval[k] < 0 || rowval[k] >= h->ndofs) return fail(TOG_ERR_ARG, "rhs row out of range");
+        if (!std::isfinite(nzval[k])) return fail(TOG_ERR_ARG, "rhs has non-finite entries");
+    }
+    std::vector<uint8_t> mask(h->nnodes);
+    TOG_CUDA(cudaMemcpyAsync(mask.data(), h->d_fixmask, h->nnodes, cudaMemcpyDeviceToHost, h->stream));
+    TOG_CUDA(cudaStreamSynchronize(h->stream));
+    if (h->mlg_cols < ncol) {
+        if (h->d_mlg) cudaFree(h->d_mlg);
+        h->d_mlg = nullptr;
+        h->mlg_cols = 0;
+        TOG_TRY(dalloc(&h->d_mlg, (size_t)ncol * h->ncells));
+        h->mlg_cols = ncol;
+    }
+    if (!h->d_fsave) TOG_TRY(dalloc(&h->d_fsave, h->ndofs));
+    const size_t fbytes = h->ndofs * sizeof(double);
+    TOG_CUDA(cudaMemcpyAsync(h->d_fsave, h->d_f, fbytes, cudaMemcpyDeviceToDevice, h->stream));
+    const double fnorm_saved = h->fnorm2;
+    long long maxnz = 1;
+    for (int i = 0; i < ncol; ++i) maxnz = std::max<long long>(maxnz, colptr[i + 1] - colptr[i]);
+    long long* d_idx = nullptr;
+    double* d_val = nullptr;
+    TOG_TRY(dalloc(&d_idx, maxnz));
+    if (dalloc(&d_val, maxnz) != TOG_OK) {
+        cudaFree(d_idx);
+        return TOG_ERR_OOM;
+    }
+    int rc = TOG_OK;
+    long long its = 0;
+    tog_solve_stats ss{};
+    std::vector<long long> idx;
+    std::vector<double> val;
+    for (int i = 0; i < ncol && (rc == TOG_OK || rc == TOG_NOT_CONVERGED); ++i) {
+        // column i with its prescribed dofs zeroed (apply_zero!), summed per internal dof
+        idx.clear();
+        val.clear();
+        std::vector<std::pair<long long, double>> ent;
+        for (long long k = colptr[i]; k < colptr[i + 1]; ++k) {
+            const long long ii = h->ref2int[rowval[k]];
+            if ((mask[ii / h->dim] >> (ii % h->dim)) & 1u) continue;
+            ent.emplace_back(ii, nzval[k]);
+        }
+        std::sort(ent.begin(), ent.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
+        double s2 = 0.0;
+        for (size_t k = 0; k < ent.size(); ++k) {
+            if (!idx.empty() && idx.back() == ent[k].first)
+                val.back() += ent[k].second;
+            else {
+                idx.push_back(ent[k].first);
+                val.push_back(ent[k].second);
+            }
+        }
+        for (double v : val) s2 += v * v;
+        h->fnorm2 = s2;
+        auto cu = [&](cudaError_t e) {
+            if (e != cudaSuccess && rc == TOG_OK) rc = fail(TOG_ERR_CUDA, cudaGetErrorString(e));
+        };
+        cu(cudaMemsetAsync(h->d_f, 0, fbytes, h->stream));
+        if (!idx.empty()) {
+            cu(cudaMemcpyAsync(d_idx, idx.data(), idx.size() * sizeof(long long), cudaMemcpyHostToDevice, h->stream));
+            cu(cudaMemcpyAsync(d_val, val.data(), val.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+            k_scatter_pairs<<<std::min<int>(1024, ((int)idx.size() + 255) / 256), 256, 0, h->stream>>>(
+                h->d_f, d_idx, d_val, (int)idx.size());
+            TOG_LAUNCHED(1);
+            cu(cudaGetLastError());
+            cu(cudaStreamSynchronize(h->stream));   // the host pairs are reused by the next column
+        }
+        if (rc != TOG_OK) break;
+        const int r = do_solve(h, precision, rtol, abstol, maxiter, 0, &ss);   // each column from zero
+        its += ss.iterations;
+        if (r != TOG_OK && r != TOG_NOT_CONVERGED) {
+            rc = r;
+            break;
+        }
+        if (r == TOG_NOT_CONVERGED) rc = r;
+        const int rc2 = compliance_dev(h, h->d_mlg + (size_t)i * h->ncells);
+        if (rc2 != TOG_OK) {
+            rc = rc2;
+            break;
+        }
+        cu(cudaMemcpyAsync(h->h_scalar, h->d_scalar, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+        cu(cudaStreamSynchronize(h->stream));
+        c[i] = h->h_scalar[0];
+    }
+    cudaStreamSynchronize(h->stream);
+    cudaFree(d_idx);
+    cudaFree(d_val);
+    // the handle's own rhs again (the displacement stays that of the last column)
+    TOG_CUDA(cudaMemcpyAsync(h->d_f, h->d_fsave, fbytes, cudaMemcpyDeviceToDevice, h->stream));
+    TOG_CUDA(cudaStreamSynchronize(h->stream));
+    h->fnorm2 = fnorm_saved;
+    if (stats) {
+        *stats = ss;
+        stats->iterations = (int32_t)std::min<long long>(its, INT32_MAX);
+    }
+    return rc;
+}
+
+int tog_multiload_gradient(tog_handle* h, int32_t ncol, const double* w, double* out) {
+    TOG_TRY(check_handle(h));
+    if (!w || !out || ncol <= 0) return fail(TOG_ERR_ARG, "need ncol > 0, w[ncol] and out[ncells]");
+    if (!h->d_mlg || ncol > h->mlg_cols) return fail(TOG_ERR_STATE, "no multi-load gradients: call tog_multiload_compliance first");
+    double* d_wc = nullptr;
+    TOG_TRY(dalloc(&d_wc, ncol));
+    TOG_CUDA(cudaMemcpyAsync(d_wc, w, ncol * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    k_weighted_cols<<<h->ew_blocks(h->ncells), kEwThreads, 0, h->stream>>>(h->d_mlg, d_wc, ncol, h->ncells, h->d_grad);
+    TOG_LAUNCHED(1);
+    const cudaError_t e = cudaGetLastError();
+    TOG_CUDA(cudaMemcpyAsync(out, h->d_grad, h->ncells * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    TOG_CUDA(cudaStreamSynchronize(h->stream));
+    cudaFree(d_wc);
+    TOG_CUDA(e);
     return TOG_OK;
 }
 

@@ -30,6 +30,7 @@ using TopOpt.Functions: ComplianceFun, VolumeFun
 using TopOpt.Utilities: PowerPenaltyFun, getpenalty
 using ChainRulesCore
 using Ferrite
+using SparseArrays
 
 export GB300Solver, GB300FEASolver, GB300DensityFilter, GB300SensFilter, oc_update!, simp_step!
 export BatchedSIMP, batch_step!, batch_results, WarmStartNet, attach_network!
@@ -154,6 +155,57 @@ function (o::ComplianceFun{T,<:GB300FEASolver})(x::PseudoDensities) where {T}
     c = Ref{Float64}(0.0)
     check(ccall((:tog_compliance, libtog), Cint, (Ptr{Cvoid}, Ref{Float64}, Ptr{Float64}), s.handle, c, o.grad))
     return c[]
+end
+
+# ---- multiple loads: MeanComplianceFun / BlockComplianceFun (src/Functions/mean_compliance.jl,
+#      block_compliance.jl) on a GB300FEASolver.  The reference's versions need the per-element
+#      Kes the GB300 solver never builds; these methods solve every rhs column on the device.
+const TF = TopOpt.Functions
+function _multiload!(s::GB300FEASolver, cols::SparseMatrixCSC)
+    length(s.vars) == getncells(s.problem) || throw(DimensionMismatch("vars"))
+    check(ccall((:tog_set_vars, libtog), Cint, (Ptr{Cvoid}, Ptr{Float64}), s.handle, s.vars))
+    c = zeros(size(cols, 2))
+    colptr = Int64.(cols.colptr .- 1)
+    rowval = Int32.(cols.rowval .- 1)
+    nzval = Vector{Float64}(cols.nzval)
+    check(ccall((:tog_multiload_compliance, libtog), Cint,
+                (Ptr{Cvoid}, Int32, Ptr{Int64}, Ptr{Int32}, Ptr{Float64}, Cint, Float64, Float64, Int32,
+                 Ptr{Float64}, Ref{SolveStats}),
+                s.handle, Int32(size(cols, 2)), colptr, rowval, nzval, s.precision, s.rtol, s.abstol,
+                Int32(s.cg_max_iter), c, s.stats))
+    return c
+end
+function _multiload_grad!(out, s::GB300FEASolver, w::AbstractVector)
+    check(ccall((:tog_multiload_gradient, libtog), Cint, (Ptr{Cvoid}, Int32, Ptr{Float64}, Ptr{Float64}),
+                s.handle, Int32(length(w)), Vector{Float64}(w), out))
+    return out
+end
+_ml_columns(m::TF.ExactMean, F) = (sparse(F), size(F, 2))
+_ml_columns(m::TF.ExactSVDMean, F) = (sparse(m.US), m.n)
+function _ml_columns(m::TF.TraceEstimationMean, F)
+    m.sample_once || m.sample_method(m.V)
+    return sparse(m.F * m.V), size(m.V, 2) * size(m.F, 2)
+end
+function _ml_columns(m::TF.TraceEstimationSVDMean, F)
+    m.sample_once || m.sample_method(m.V)
+    return sparse(m.US * m.V), size(m.V, 2) * m.n
+end
+function (ec::TF.MeanComplianceFun{T,<:ComplianceFun{T,<:GB300FEASolver}})(x::PseudoDensities) where {T}
+    s = ec.compliance.solver
+    s.vars .= x.x
+    cols, n = _ml_columns(ec.method, ec.F)
+    c = _multiload!(s, cols)
+    _multiload_grad!(ec.grad, s, fill(1.0 / n, size(cols, 2)))
+    return sum(c) / n
+end
+function TF.compute_block_compliance(bc::TF.BlockComplianceFun{T,<:ComplianceFun{T,<:GB300FEASolver}},
+                                     m::TF.ExactDiagonal) where {T}
+    bc.raw_val .= _multiload!(bc.compliance.solver, sparse(m.F))
+    return bc.raw_val
+end
+function TF.compute_jtvp!_bc(out, bc::TF.BlockComplianceFun{T,<:ComplianceFun{T,<:GB300FEASolver}},
+                             m::TF.ExactDiagonal, w) where {T}
+    return _multiload_grad!(out, bc.compliance.solver, w)
 end
 
 function TopOpt.Functions.VolumeFun(s::GB300FEASolver{T}; fraction=true) where {T}

@@ -320,6 +320,205 @@ class VolumeFun:
         return self.grad * delta
 
 
+# --------------------------------------------------------------------------- multiple loads
+class MultiLoad:
+    """MultiLoad(problem, F) (src/TopOptProblems/multiload.jl:21-46): a structured problem
+    with a load matrix F (ndofs x nscenarios, scipy sparse or dense, 0-based reference dof
+    rows) in place of its single load.  MultiLoad(problem, N, load_rules) builds F from
+    [(position, f)] pairs, f() returning the load vector of one scenario, placed on the dofs
+    of the node nearest to position (find_nearest_dofs, multiload.jl:48-61).  Other
+    attributes are the base problem's."""
+
+    def __init__(self, problem, F, load_rules=None):
+        import scipy.sparse as sp
+        self.problem = problem
+        if load_rules is not None:
+            N = int(F)
+            I, J, V = [], [], []
+            for pos, f in load_rules:
+                dofs = find_nearest_dofs(problem, pos)
+                for i in range(N):
+                    load = np.asarray(f(), dtype=np.float64)
+                    I.extend(dofs.tolist())
+                    J.extend([i] * len(dofs))
+                    V.extend(load.tolist())
+            F = sp.csc_matrix((V, (I, J)), shape=(problem.ndofs, N))
+        self.F = sp.csc_matrix(F, dtype=np.float64)
+        if self.F.shape[0] != problem.ndofs:
+            raise ValueError("DimensionMismatch: F must have one row per dof")
+
+    def __getattr__(self, name):
+        return getattr(self.__dict__["problem"], name)
+
+
+def find_nearest_dofs(problem, pos):
+    """The dofs of the node nearest to pos (multiload.jl:48-61)."""
+    ix, iy, iz = problem._node_grid()
+    coords = np.stack([ix * problem.sizes[0], iy * problem.sizes[1]] +
+                      ([iz * problem.sizes[2]] if problem.dim == 3 else []), axis=1)
+    d = np.linalg.norm(coords - np.asarray(pos, dtype=np.float64)[None, :], axis=1)
+    return problem.node_dofs[int(np.argmin(d))]
+
+
+def generate_scenarios(dof, size, f, perturb=None, rng=None):
+    """Sparse ndofs x nscenarios load matrix with load f (1 + perturb()) at the single dof
+    `dof` (0-based) in every scenario (mean_compliance.jl:209-219); perturb defaults to
+    U(-0.5, 0.5) from a seeded numpy generator."""
+    import scipy.sparse as sp
+    ndofs, ns = size
+    if perturb is None:
+        g = rng if rng is not None else np.random.default_rng(0)
+        perturb = lambda: g.random() - 0.5   # noqa: E731
+    V = [f * (1.0 + perturb()) for _ in range(ns)]
+    return sp.csc_matrix((V, ([dof] * ns, list(range(ns)))), shape=(ndofs, ns))
+
+
+def hutch_rand(V, rng=None):
+    """Rademacher (+-1) samples into V (hutch_rand!, mean_compliance.jl:151-158)."""
+    g = rng if rng is not None else np.random.default_rng(0)
+    V[...] = g.choice(np.array([-1.0, 1.0]), size=V.shape)
+    return V
+
+
+def hadamard(V):
+    """Hadamard (+-1) columns into V (hadamard!, mean_compliance.jl:186-197): the first nv
+    columns of a Sylvester matrix, its rows repeated down to n."""
+    n, nv = V.shape
+    H = np.ones((1, 1))
+    while H.shape[0] < nv:
+        H = np.block([[H, H], [H, -H]])
+    H = H[:, :nv]
+    H = np.tile(H, (int(np.ceil(n / nv)), 1))
+    V[...] = H[:n, :]
+    return V
+
+
+def _svd_columns(F):
+    """US of the thin SVD of F's nonzero rows, singular values > 1e-6 (ExactSVDMean,
+    src/Functions/trace.jl:15-34)."""
+    import scipy.sparse as sp
+    rows = np.unique(F.indices)
+    Fc = F[rows, :].toarray()
+    U, S, _ = np.linalg.svd(Fc, full_matrices=False)
+    keep = np.nonzero(S > 1e-6)[0]
+    US = U[:, keep] * S[keep]
+    out = np.zeros((F.shape[0], len(keep)))
+    out[rows, :] = US
+    return sp.csc_matrix(out)
+
+
+class _MultiLoadSolves:
+    def __init__(self, solver):
+        self.solver = solver
+        self.last_stats = None
+
+    def solve(self, cols, x, precision=None):
+        """Per-column compliance f_i' K(x)^-1 f_i of the CSC columns at densities x (the
+        column gradients stay on the device)."""
+        s = self.solver
+        s.vars = np.asarray(x.x if isinstance(x, PseudoDensities) else x, dtype=np.float64).copy()
+        s._push_vars()
+        cols = cols.tocsc()
+        cols.sort_indices()
+        colptr = np.ascontiguousarray(cols.indptr, dtype=np.int64)
+        rowval = np.ascontiguousarray(cols.indices, dtype=np.int32)
+        nzval = np.ascontiguousarray(cols.data, dtype=np.float64)
+        c = np.empty(cols.shape[1])
+        st = L.SolveStats()
+        L.check(L.lib().tog_multiload_compliance(s.handle, cols.shape[1], colptr.ctypes.data_as(L._I64),
+                                                 L.iptr(rowval), L.dptr(nzval),
+                                                 PRECISIONS[precision or s.precision], s.rtol, s.abstol,
+                                                 s.cg_max_iter, L.dptr(c), L.C.byref(st)))
+        self.last_stats = st
+        return c
+
+    def gradient(self, w):
+        w = np.ascontiguousarray(w, dtype=np.float64)
+        out = np.empty(self.solver.problem.ncells)
+        L.check(L.lib().tog_multiload_gradient(self.solver.handle, len(w), L.dptr(w), L.dptr(out)))
+        return out
+
+
+class MeanComplianceFun:
+    """Mean compliance over the load cases of a MultiLoad problem (mean_compliance.jl:8-150):
+    method "exact" (every column of F), "exact_svd" (the columns U S of F's thin SVD; the
+    default), "trace" (Hutchinson / Hadamard estimation with nv probe vectors: the columns
+    F v) or "trace_svd" (the same on U S).  The solves, compliances and gradients run on the
+    device; F's SVD and the probes are set up once on the host, as in the reference."""
+
+    def __init__(self, problem, solver, method="exact_svd", sample_once=True, nv=None, V=None,
+                 sample_method="hutch", rng=None):
+        if not isinstance(problem, MultiLoad):
+            raise ValueError("MeanComplianceFun needs a MultiLoad problem")
+        self.F, self.n = problem.F, problem.F.shape[1]
+        self.method, self.sample_once = method, sample_once
+        self.rng = rng if rng is not None else np.random.default_rng(0)
+        self._ml = _MultiLoadSolves(solver)
+        self.solver = solver
+        if method == "exact":
+            self.base, self.V = self.F, None
+        elif method == "exact_svd":
+            self.base, self.V = _svd_columns(self.F), None
+        elif method in ("trace", "approx", "trace_svd"):
+            self.base = self.F if method != "trace_svd" else _svd_columns(self.F)
+            self.sampler = hadamard if sample_method == "hadamard" else (lambda A: hutch_rand(A, self.rng))
+            if V is None:   # probes sampled at construction (and again per call unless sample_once)
+                self.V = np.zeros((self.base.shape[1], 1 if nv is None else int(nv)))
+                self.sampler(self.V)
+            else:
+                V = np.asarray(V, dtype=np.float64)
+                self.V = V[:, :(V.shape[1] if nv is None else int(nv))].copy()
+            if method == "trace_svd" and sample_method == "hadamard":
+                self.sample_once = True
+        else:
+            raise ValueError("method must be exact, exact_svd, trace or trace_svd")
+        self.grad = np.zeros(solver.problem.ncells)
+
+    def _columns(self):
+        import scipy.sparse as sp
+        if self.V is None:
+            return self.base, self.n
+        if not self.sample_once:
+            self.sampler(self.V)
+        return sp.csc_matrix(self.base @ self.V), self.V.shape[1] * self.n
+
+    def __call__(self, x):
+        cols, div = self._columns()
+        c = self._ml.solve(cols, x)
+        self.grad = self._ml.gradient(np.full(cols.shape[1], 1.0 / div))
+        return float(np.sum(c) / div)
+
+    def pullback(self, delta=1.0):
+        return self.grad * delta
+
+
+class BlockComplianceFun:
+    """The vector of per-load-case compliances f_i' K^-1 f_i of a MultiLoad problem
+    (block_compliance.jl:7-110, method "exact"); pullback(delta) = sum_i delta_i dc_i/dx."""
+
+    def __init__(self, problem, solver, method="exact"):
+        if not isinstance(problem, MultiLoad):
+            raise ValueError("BlockComplianceFun needs a MultiLoad problem")
+        if method != "exact":
+            raise ValueError("BlockComplianceFun: only method exact is provided")
+        self.F = problem.F
+        self._ml = _MultiLoadSolves(solver)
+        self.solver = solver
+        self.val = np.zeros(self.F.shape[1])
+        self.fevals = 0
+
+    def __call__(self, x):
+        self.fevals += 1
+        self.val = self._ml.solve(self.F, x)
+        return self.val.copy()
+
+    def pullback(self, delta):
+        d = np.asarray(delta, dtype=np.float64)
+        if d.shape != (self.F.shape[1],):
+            raise ValueError("DimensionMismatch: BlockComplianceFun pullback expects one weight per load case")
+        return self._ml.gradient(d)
+
+
 class _NodeFilter:
     def __init__(self, solver, rmin):
         self.solver = solver
