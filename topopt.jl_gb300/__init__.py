@@ -7,6 +7,7 @@ Import it as ``topopt_gb300`` (see ``load()`` in the repository's
 __graft_entry__.py; the directory name carries a dot).
 """
 from ._lib import TopOptError, NotConverged, lib  # noqa: F401
+from .vtk import save_mesh  # noqa: F401
 from .topopt_api import (  # noqa: F401
     BatchedSIMP,
     BlockComplianceFun,
