@@ -50,6 +50,7 @@ enum tog_filter_op { TOG_FILTER_J = 0, TOG_FILTER_JT = 1 };
 enum tog_projection_kind { TOG_PROJ_HEAVISIDE = 1, TOG_PROJ_SIGMOID = 2 };
 enum tog_element_state { TOG_ELEM_FREE = 0, TOG_ELEM_BLACK = 1, TOG_ELEM_WHITE = 2 };
 enum tog_optimizer { TOG_OPT_OC = 0, TOG_OPT_MMA = 1 };
+enum tog_convergence { TOG_CONV_DEFAULT = 0, TOG_CONV_ENERGY = 1 };
 
 typedef struct tog_handle tog_handle;
 
@@ -119,6 +120,14 @@ int tog_set_fixed_dofs(tog_handle* h, int64_t n, const int32_t* dofs);
 /* globalinfo.f, dense, reference dof order (matrices_and_vectors.jl:346-365). */
 int tog_set_rhs(tog_handle* h, const double* f);
 /* setpenalty!(solver, p) (solvers_api.jl:417-427). */
+/* The PCG stop rule, FEASolver's conv keyword (src/FEA/solvers_api.jl:482):
+ * TOG_CONV_DEFAULT stops on the recurrence residual norm (IterativeSolvers' default), and
+ * TOG_CONV_ENERGY on EnergyCriteria (src/FEA/convergence_criteria.jl:26-45): the relative
+ * change of x'Ax and |x'r| / x'Ax both <= max(rtol ||r0||, abstol), checked on the start
+ * vector and after every iteration; a NaN or negative x'Ax gives TOG_BREAKDOWN (the
+ * reference's DomainError).  EnergyCriteria applies to TOG_FP64 solves; TOG_FP32_IR
+ * rejects it with TOG_ERR_ARG. */
+int tog_set_convergence(tog_handle* h, int32_t criteria);
 int tog_set_penalty(tog_handle* h, double p);
 /* solver.vars .= x  (compliance.jl:65): the filtered pseudo-densities, one per cell. */
 int tog_set_vars(tog_handle* h, const double* x);

@@ -356,10 +356,12 @@ def jacobi_diag(st: FEAState):
 
 
 def pcg(st: FEAState, f=None, rtol=math.sqrt(np.finfo(np.float64).eps), abstol=0.0,
-        maxiter=700, x0=None, precond=True):
+        maxiter=700, x0=None, precond=True, conv="default"):
     """Jacobi PCG as IterativeSolvers.cg! (called from solvers_api.jl:177-220):
     tol = max(rtol*||r0||, abstol); stop when the recurrence residual norm <= tol
-    or after maxiter iterations.  Returns (x, iterations, ||r||)."""
+    or after maxiter iterations.  conv="energy" replaces the stop test by EnergyCriteria's
+    isconverged (src/FEA/convergence_criteria.jl:26-45), checked before every iteration
+    as IterativeSolvers does.  Returns (x, iterations, ||r||)."""
     f = st.prob.f if f is None else f
     b = f.copy()
     b[~st.free_mask] = 0.0
@@ -371,7 +373,22 @@ def pcg(st: FEAState, f=None, rtol=math.sqrt(np.finfo(np.float64).eps), abstol=0
     u = np.zeros_like(b)
     rho = 1.0
     it = 0
-    while it < maxiter and res > tol:
+    energy = [0.0]
+
+    def converged():
+        if conv != "energy":
+            return res <= tol
+        xtr = float(x @ r)
+        xAx = float(b @ x) - xtr
+        dE = xAx - energy[0]
+        if math.isnan(dE) or math.isnan(xAx) or xAx < 0:
+            raise FloatingPointError("EnergyCriteria: NaN or negative x'Ax")
+        with np.errstate(divide="ignore", invalid="ignore"):
+            ok = bool(np.float64(abs(dE)) / xAx <= tol and np.float64(abs(xtr)) / xAx <= tol)
+        energy[0] = xAx
+        return ok
+
+    while it < maxiter and not converged():
         c = dinv * r
         rho_prev, rho = rho, float(c @ r)
         beta = rho / rho_prev

@@ -282,3 +282,19 @@ def test_mean_compliance_svd_equals_exact_and_fd(O):
         xp[e] += h
         fd = (O.mean_compliance(st, F, xp, "exact")[0] - m1) / h
         assert abs(fd - g1[e]) < 1e-4 * max(1.0, abs(g1[e]))
+
+
+def test_energy_criteria_stop_rule(O):
+    """EnergyCriteria (src/FEA/convergence_criteria.jl:26-45): the oracle's PCG stops once
+    the relative change of x'Ax and |x'r| / x'Ax are within tol, with a solution that
+    agrees with the direct solve (the reference's solver-agreement bar, 1e-4)."""
+    prob = O.point_load_cantilever((12, 6), (1.0, 1.0))
+    st = O.fea_setup(prob, xmin=1e-3, p=3.0)
+    st.vars = np.random.default_rng(1).uniform(0.3, 1.0, prob.grid.ncells)
+    ud = O.direct_solve(st)
+    u, its, _ = O.pcg(st, rtol=1e-8, maxiter=10000, conv="energy")
+    assert 0 < its < 10000
+    assert np.linalg.norm(u - ud) / np.linalg.norm(ud) < 1e-4
+    # the residual-norm rule on the same system stops elsewhere, at the same solution
+    u2, its2, _ = O.pcg(st, rtol=1e-8, maxiter=10000)
+    assert its2 > 0 and np.linalg.norm(u2 - ud) / np.linalg.norm(ud) < 1e-4

@@ -12,7 +12,9 @@ from .topopt_api import (  # noqa: F401
     BatchedSIMP,
     BlockComplianceFun,
     ComplianceFun,
+    DefaultCriteria,
     DensityFilterFun,
+    EnergyCriteria,
     FEASolver,
     FixedElementProjectorFun,
     GB300FEASolver,

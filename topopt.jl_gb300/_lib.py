@@ -14,6 +14,7 @@ TOG_FP64, TOG_FP32_IR = 0, 1
 TOG_PROJ_HEAVISIDE, TOG_PROJ_SIGMOID = 1, 2
 TOG_ELEM_FREE, TOG_ELEM_BLACK, TOG_ELEM_WHITE = 0, 1, 2
 TOG_OPT_OC, TOG_OPT_MMA = 0, 1
+TOG_CONV_DEFAULT, TOG_CONV_ENERGY = 0, 1
 TOG_FILTER_NONE, TOG_FILTER_DENSITY, TOG_FILTER_SENS = 0, 1, 2
 TOG_FILTER_J, TOG_FILTER_JT = 0, 1
 
@@ -107,6 +108,7 @@ SIGNATURES = {
     "tog_fixed_element_pullback": (C.c_int, [_H, _D, _D]),
     "tog_mma_update": (C.c_int, [_H, _D, _D, C.c_double, _D, C.c_double, _D, _D, _D]),
     "tog_mma_reset": (C.c_int, [_H]),
+    "tog_set_convergence": (C.c_int, [_H, C.c_int32]),
     "tog_multiload_compliance": (C.c_int, [_H, C.c_int32, _I64, _I32, _D, C.c_int32, C.c_double, C.c_double,
                                            C.c_int32, _D, C.c_void_p]),
     "tog_multiload_gradient": (C.c_int, [_H, C.c_int32, _D, _D]),

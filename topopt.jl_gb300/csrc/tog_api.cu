@@ -161,6 +161,8 @@ struct tog_handle {
     double* d_side64[8] = {};
     // graphs
     cudaGraphExec_t g_pcg64 = nullptr, g_pcg32 = nullptr, g_oc = nullptr;
+    cudaGraphExec_t g_pcg64e = nullptr;   // FP64 batch with the EnergyCriteria check
+    int conv = TOG_CONV_DEFAULT;
     int graph_nodes64 = 0, graph_nodes32 = 0;
 
     Dims dims() const {
@@ -421,13 +423,18 @@ void launch_pcg_init(tog_handle* h, cudaStream_t s, int zero_x, double rtol, dou
 // read the iteration state from device memory and return at once after
 // convergence, so one graph serves every batch of every solve.
 template <typename T>
-int build_pcg_graph(tog_handle* h, cudaGraphExec_t* out) {
+int build_pcg_graph(tog_handle* h, cudaGraphExec_t* out, bool energy = false) {
     cudaGraph_t g = nullptr;
     TOG_CUDA(cudaStreamBeginCapture(h->own, cudaStreamCaptureModeThreadLocal));
     const long long before = g_launches.load();
     for (int i = 0; i < kPcgBatch; ++i) {
         launch_matvec<T, MV_PCG>(h, h->own, nullptr, nullptr, nullptr);
         launch_pcg_update<T>(h, h->own);
+        if (energy) {
+            k_energy_check<<<h->ew_blocks(h->ndofs), kEwThreads, 0, h->own>>>(h->d_u, h->d_r64, h->d_f, h->ndofs,
+                                                                             h->d_st64, h->d_partials);
+            TOG_LAUNCHED(1);
+        }
     }
     // kernels per batch; captured launches run only when the graph is launched
     const int nodes = (int)(g_launches.load() - before);
@@ -447,10 +454,10 @@ int sync_state(tog_handle* h, const PcgState* d_st) {
 
 // Run graph batches until the PCG state says done.
 template <typename T>
-int run_pcg(tog_handle* h) {
-    cudaGraphExec_t* g = std::is_same<T, double>::value ? &h->g_pcg64 : &h->g_pcg32;
+int run_pcg(tog_handle* h, bool energy = false) {
+    cudaGraphExec_t* g = std::is_same<T, double>::value ? (energy ? &h->g_pcg64e : &h->g_pcg64) : &h->g_pcg32;
     PcgState* d_st = std::is_same<T, double>::value ? h->d_st64 : h->d_st32;
-    if (!*g) TOG_TRY(build_pcg_graph<T>(h, g));
+    if (!*g) TOG_TRY(build_pcg_graph<T>(h, g, energy));
     TOG_TRY(sync_state(h, d_st));
     while (!h->h_st->done) {
         TOG_CUDA(cudaGraphLaunch(*g, h->stream));
@@ -487,8 +494,15 @@ int solve_fp64(tog_handle* h, double rtol, double abstol, int maxit, int warm, t
         TOG_CUDA(cudaMemcpyAsync(h->d_r64, h->d_f, h->ndofs * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
         launch_pcg_init<double>(h, h->stream, 1, rtol, abstol, h->fnorm2, maxit);
     }
+    const bool energy = h->conv == TOG_CONV_ENERGY;
+    if (energy) {   // the stop rule of EnergyCriteria, first checked on the start vector
+        k_energy_init<<<1, 32, 0, h->stream>>>(h->d_st64);
+        k_energy_check<<<h->ew_blocks(h->ndofs), kEwThreads, 0, h->stream>>>(h->d_u, h->d_r64, h->d_f, h->ndofs,
+                                                                            h->d_st64, h->d_partials);
+        TOG_LAUNCHED(2);
+    }
     TOG_CUDA(cudaGetLastError());
-    TOG_TRY(run_pcg<double>(h));
+    TOG_TRY(run_pcg<double>(h, energy));
     h->u_valid = true;
     const PcgState& s = *h->h_st;
     if (st) {
@@ -498,6 +512,8 @@ int solve_fp64(tog_handle* h, double rtol, double abstol, int maxit, int warm, t
         st->abs_residual = std::sqrt(s.rr);
         st->rel_residual = h->fnorm2 > 0 ? std::sqrt(s.rr / h->fnorm2) : std::sqrt(s.rr);
     }
+    if (s.status == 7)
+        return fail(TOG_BREAKDOWN, "EnergyCriteria: NaN or negative x'Ax (the reference's DomainError)");
     return s.status == 0 ? TOG_OK : fail(s.status, s.status == 3 ? "PCG did not converge within maxiter"
                                                                    : "PCG breakdown (p'Kp <= 0 or NaN)");
 }
@@ -808,6 +824,9 @@ __global__ void k_projection(int kind, double beta, const double* __restrict__ x
 
 int do_solve(tog_handle* h, int prec, double rtol, double abstol, int maxit, int warm, tog_solve_stats* st) {
     TOG_TRY(refresh_scales(h));
+    if (prec == TOG_FP32_IR && h->conv == TOG_CONV_ENERGY)
+        return fail(TOG_ERR_ARG, "EnergyCriteria is a stop rule of the FP64 solve (FP32-IR stops on the FP64 "
+                                 "true residual)");
     if (prec == TOG_FP64) return solve_fp64(h, rtol, abstol, maxit, warm, st);
     if (prec == TOG_FP32_IR) return solve_fp32_ir(h, rtol, abstol, maxit, warm, st);
     return fail(TOG_ERR_ARG, "unknown precision");
@@ -1257,6 +1276,7 @@ int tog_destroy(tog_handle* h) {
     if (h->stream && h->stream != h->own) cudaStreamSynchronize(h->stream);
     if (h->g_pcg64) cudaGraphExecDestroy(h->g_pcg64);
     if (h->g_pcg32) cudaGraphExecDestroy(h->g_pcg32);
+    if (h->g_pcg64e) cudaGraphExecDestroy(h->g_pcg64e);
     if (h->g_oc) cudaGraphExecDestroy(h->g_oc);
     if (h->g_mma) cudaGraphExecDestroy(h->g_mma);
     if (h->h_mma) cudaFreeHost(h->h_mma);
@@ -1323,6 +1343,13 @@ int tog_set_rhs(tog_handle* h, const double* f) {
     h->fnorm2 = s;
     TOG_CUDA(cudaMemcpyAsync(h->d_f, fi.data(), h->ndofs * sizeof(double), cudaMemcpyHostToDevice, h->stream));
     TOG_CUDA(cudaStreamSynchronize(h->stream));
+    return TOG_OK;
+}
+
+int tog_set_convergence(tog_handle* h, int32_t criteria) {
+    TOG_TRY(check_handle(h));
+    if (criteria != TOG_CONV_DEFAULT && criteria != TOG_CONV_ENERGY) return fail(TOG_ERR_ARG, "unknown criteria");
+    h->conv = criteria;
     return TOG_OK;
 }
 

@@ -52,10 +52,16 @@ struct PcgState {
     int done;        // 1 = stop (converged, breakdown or maxit)
     int maxit;
     int status;      // 0 running/converged, 3 = not converged at maxit, 4 = breakdown,
-                     // 6 = paused for a reliable update
+                     // 6 = paused for a reliable update, 7 = EnergyCriteria domain error
     unsigned cnt[4]; // last-block counters
     double rr_max;   // largest ||r||^2 since the last reliable update
     double ru_delta2;// pause when ||r||^2 < ru_delta2 * rr_max (0 = never)
+    // EnergyCriteria (FP64 solves): x'Ax at the last check, its tolerance, the iteration
+    // the last check saw
+    double energy;
+    double tol_e;
+    int it_e;
+    int pad_e;
 };
 
 struct OcState {

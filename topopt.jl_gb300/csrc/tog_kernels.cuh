@@ -388,6 +388,55 @@ __global__ void __launch_bounds__(256) k_pcg_update(T* __restrict__ x, T* __rest
     }
 }
 
+// EnergyCriteria (src/FEA/convergence_criteria.jl:26-45), IterativeSolvers' isconverged
+// for it: with xr = x'r and x'Ax = f'x - xr, converged when |x'Ax - E| / x'Ax <= tol and
+// |xr| / x'Ax <= tol, E the value of the previous check, which it then replaces; a NaN
+// or a negative x'Ax is the reference's DomainError (status 7).  Runs once per completed
+// iteration (and once on the start vector), after the update, on FP64 dof arrays.
+__global__ void k_energy_init(PcgState* st) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        st->tol_e = sqrt(fmax(st->tol2, 0.0));   // max(rtol ||r0||, abstol)
+        st->tol2 = -1.0;                         // no residual-norm stop
+        st->energy = 0.0;
+        st->it_e = -1;
+        st->done = st->maxit <= 0 ? 1 : 0;
+        st->status = st->maxit <= 0 ? 3 : 0;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_energy_check(const double* __restrict__ x, const double* __restrict__ r,
+                                                      const double* __restrict__ f, long long n, PcgState* st,
+                                                      double* partials) {
+    const int it = st->it;
+    if (it == st->it_e || st->status == 7) return;   // nothing new since the last check
+    double xr = 0.0, fx = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const double xi = x[i];
+        xr = fma(xi, r[i], xr);
+        fx = fma(f[i], xi, fx);
+    }
+    double v[2] = {xr, fx}, tot[2];
+    if (grid_reduce_last<2>(v, partials, &st->cnt[3], tot)) {
+        if (threadIdx.x == 0) {
+            const double xAx = tot[1] - tot[0];
+            const double dE = xAx - st->energy;
+            st->it_e = it;
+            if (isnan(dE) || isnan(xAx) || xAx < 0.0) {
+                st->status = 7;
+                st->done = 1;
+            } else {
+                const bool conv = fabs(dE) / xAx <= st->tol_e && fabs(tot[0]) / xAx <= st->tol_e;
+                st->energy = xAx;
+                if (conv && st->status != 4) {
+                    st->status = 0;
+                    st->done = 1;
+                }
+            }
+        }
+    }
+}
+
 // Start a PCG solve from the residual already stored in r (x either zeroed here
 // or holding the warm start).  tol2 = max(rtol^2 * bnorm2, abstol^2), with
 // bnorm2 < 0 meaning "use ||r0||^2".

@@ -103,7 +103,7 @@ plus `rtol` (IterativeSolvers' reltol, exposed) and `precision` (`:fp64` or
 function TopOpt.FEA.FEASolver(::Type{GB300Solver}, problem::StiffnessTopOptProblem{dim,T};
                               xmin=T(1) / 1000, penalty=PowerPenaltyFun{T}(1), cg_max_iter=700,
                               abstol=T(1e-7), rtol=sqrt(eps(T)), precision=:fp64, warm_start=false,
-                              kwargs...) where {dim,T}
+                              conv=TopOpt.FEA.DefaultCriteria(), kwargs...) where {dim,T}
     ch = problem.ch
     any(!=(0), ch.inhomogeneities) && throw(ArgumentError(
         "GB300Solver supports homogeneous Dirichlet BCs only (as CGMatrixFreeSolver)"))
@@ -118,6 +118,9 @@ function TopOpt.FEA.FEASolver(::Type{GB300Solver}, problem::StiffnessTopOptProbl
     check(ccall((:tog_set_fixed_dofs, libtog), Cint, (Ptr{Cvoid}, Int64, Ptr{Int32}), h[], length(fixed), fixed))
     f = Vector{Float64}(TopOpt.TopOptProblems.make_cload(problem))
     check(ccall((:tog_set_rhs, libtog), Cint, (Ptr{Cvoid}, Ptr{Float64}), h[], f))
+    # conv (solvers_api.jl:482): EnergyCriteria runs as the FP64 solve's stop rule on the device
+    check(ccall((:tog_set_convergence, libtog), Cint, (Ptr{Cvoid}, Int32), h[],
+                conv isa TopOpt.FEA.EnergyCriteria ? Int32(1) : Int32(0)))
     nc = getncells(problem)
     prec = precision === :fp32_ir ? TOG_FP32_IR : TOG_FP64
     s = GB300FEASolver{T,typeof(problem)}(problem, h[], ones(T, nc), zeros(T, length(f)), penalty, T(xmin),

@@ -150,6 +150,17 @@ class PseudoDensities:
         self.x = np.ascontiguousarray(x, dtype=np.float64)
 
 
+class DefaultCriteria:
+    """The residual-norm stop of IterativeSolvers' cg! (src/FEA/convergence_criteria.jl:13)."""
+    code = L.TOG_CONV_DEFAULT
+
+
+class EnergyCriteria:
+    """EnergyCriteria (src/FEA/convergence_criteria.jl:20-45): stop when the relative change
+    of x'Ax and |x'r| / x'Ax are both within the solve tolerance (FP64 solves)."""
+    code = L.TOG_CONV_ENERGY
+
+
 class GB300Solver:
     """Marker type: FEASolver(GB300Solver, problem; ...) -- the AbstractLinearSolver
     slot of solvers_api.jl:44 filled by libtopopt_gb300."""
@@ -165,7 +176,7 @@ class GB300FEASolver:
     cg_max_iter = 700, abstol = 1e-7, rtol = sqrt(eps) (IterativeSolvers' reltol)."""
 
     def __init__(self, problem, *, xmin=None, penalty=None, cg_max_iter=700, abstol=None, rtol=None,
-                 precision="fp64", warm_start=False):
+                 precision="fp64", warm_start=False, conv=None):
         self.problem = problem
         self.xmin = 1e-3 if xmin is None else float(xmin)
         self.penalty = PowerPenaltyFun(1.0) if penalty is None else penalty
@@ -194,6 +205,9 @@ class GB300FEASolver:
         L.check(L.lib().tog_set_fixed_dofs(h, len(fd), L.iptr(fd)))
         f = np.ascontiguousarray(problem.load_vector())
         L.check(L.lib().tog_set_rhs(h, L.dptr(f)))
+        # conv = DefaultCriteria() (solvers_api.jl:482) or EnergyCriteria()
+        self.conv = DefaultCriteria() if conv is None else conv
+        L.check(L.lib().tog_set_convergence(h, self.conv.code))
         self.vars = np.ones(problem.ncells)          # solvers_api.jl:502
         self.last_stats = None
 
