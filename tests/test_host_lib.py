@@ -105,3 +105,36 @@ def test_fixed_element_projector_host_logic(tg):
     assert r.nel == 60 and tg.get_free_variable_count(r) == 50
     with pytest.raises(RuntimeError):   # the projection itself runs on a solver's device
         r(np.full(50, 0.5))
+
+
+def test_multiload_host_setup(tg, O):
+    """MultiLoad's load matrix from rules (multiload.jl:31-46, find_nearest_dofs :48-61),
+    generate_scenarios (mean_compliance.jl:209-219) and the SVD columns of
+    MeanComplianceFun's exact_svd method (trace.jl:15-34): host logic, no device call."""
+    import scipy.sparse as sp
+    from topopt_gb300 import topopt_api as api
+    p = tg.PointLoadCantilever((10, 6), (1.0, 1.0))
+    op = O.point_load_cantilever((10, 6), (1.0, 1.0))
+    # nearest node of (9.6, 3.2) is (10, 3); its dofs in the reference (Ferrite) numbering
+    # (the oracle keeps node_dofs as (dim, nnodes), as the reference)
+    nid = 10 + 11 * 3
+    assert list(tg.find_nearest_dofs(p, (9.6, 3.2))) == list(op.node_dofs[:, nid])
+    mags = iter([1.0, 2.0, 3.0])
+    ml = tg.MultiLoad(p, 3, [((10.0, 3.0), lambda: np.array([0.0, -next(mags)]))])
+    F = ml.F.toarray()
+    assert F.shape == (p.ndofs, 3) and ml.ncells == p.ncells
+    assert np.array_equal(F[op.node_dofs[1, nid]], [-1.0, -2.0, -3.0])
+    assert np.count_nonzero(F) == 3
+    G = tg.generate_scenarios(5, (p.ndofs, 4), 2.0, perturb=lambda: 0.25).toarray()
+    assert np.array_equal(G[5], [2.5] * 4) and np.count_nonzero(G) == 4
+    # exact_svd: F F' is preserved by the U S columns (so is tr(F' K^-1 F))
+    rng = np.random.default_rng(0)
+    Fr = np.zeros((p.ndofs, 6))
+    Fr[[3, 17, 40], :] = rng.standard_normal((3, 6))
+    US = api._svd_columns(sp.csc_matrix(Fr)).toarray()
+    assert US.shape[1] == 3
+    assert np.allclose(US @ US.T, Fr @ Fr.T, atol=1e-12)
+    with pytest.raises(ValueError):
+        tg.MultiLoad(p, sp.csc_matrix((p.ndofs + 1, 2)))
+    with pytest.raises(ValueError):
+        tg.MeanComplianceFun(p, None)
