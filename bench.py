@@ -198,7 +198,7 @@ def batch_leg(tg, stream, peaks, src, steps):
     node, volume fraction and filter radius drawn from seed 0), every design iteration
     of all problems one graph launch; FP32-IR with previous-step warm start, rtol 1e-8."""
     import torch
-    P = tg.config3_problems(256, seed=0)
+    P = tg.uneven_cantilever_set(256, seed=0)
     b = tg.BatchedSIMP(P["nelx"], P["nely"], P["load_j"], P["volfrac"], P["rmin"], rtol=1e-8)
     rows = b.autotune()
     b.set_stream(stream.cuda_stream)
@@ -490,6 +490,22 @@ def run_profile(args):
     return 0
 
 
+def run_profile_batch(args):
+    """Profiling driver of the batched 2D operator: the benchmark's 256 uneven cantilevers,
+    the band height pinned to args.profile_batch rows, five launches of the FP32 operator
+    over all problems and five of the update, outside the graph (ncu cannot profile kernels
+    inside conditional graph nodes); no timing, used under ncu."""
+    import __graft_entry__ as ge
+    tg = ge.load()
+    P = tg.uneven_cantilever_set(256, seed=0)
+    b = tg.BatchedSIMP(P["nelx"], P["nely"], P["load_j"], P["volfrac"], P["rmin"], rtol=1e-8)
+    b.set_tile_rows(int(args.profile_batch))
+    for k in (0, 1):
+        b.bench_kernel(k, 5)
+    print("batch profile driver ok", int(args.profile_batch))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -500,9 +516,13 @@ def main():
     ap.add_argument("--no-extra", action="store_true", help="skip the e2e, accuracy, FP64 and roofline legs")
     ap.add_argument("--profile", action="store_true", help="run the small ncu driver instead of the benchmark")
     ap.add_argument("--nels", default="256,128,128", help="grid of --profile")
+    ap.add_argument("--profile-batch", type=int, default=0, metavar="ROWS",
+                    help="run the batched-operator ncu driver with this band height instead of the benchmark")
     args = ap.parse_args()
     if args.profile:
         return run_profile(args)
+    if args.profile_batch:
+        return run_profile_batch(args)
     if args.warmup < 3:
         log("warmup raised to 3 (timing rule)")
         args.warmup = 3

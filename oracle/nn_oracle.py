@@ -1,7 +1,7 @@
 """Oracle of the learned warm-start network (test infrastructure only): the
 architecture of topopt.jl_gb300/csrc/tog_nn.cu restated with torch on the CPU
-in float64, used as the checker of the GPU forward pass and of the gradients of
-the GPU backward pass.  The network has no counterpart in TopOpt.jl.
+in float64, used to check the GPU forward pass and the gradients of the
+GPU backward pass.  The network has no counterpart in TopOpt.jl.
 
 Layout conventions shared with the library: tensors are channels-last
 (batch, z, y, x, channels); the parameter vector holds, per layer,

@@ -1,6 +1,6 @@
 """CPU oracle for the SIMP compliance loop of TopOpt.jl (TEST INFRASTRUCTURE ONLY).
 
-This module is the checker, not the product.  Only ``tests/``,
+This module is test infrastructure, not the product.  Only ``tests/``,
 ``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py`` may import
 it.  It restates, in plain numpy/scipy FP64, the reference algorithm of each
 step on the hot path; every function cites the TopOpt.jl file:line it follows

@@ -48,7 +48,7 @@ def test_batch_matches_single_problems(tg, autotune):
 
 
 def test_batch_matches_oracle_off_centre_load(tg, O):
-    """A load node away from mid-height (config 3 draws it on the whole right edge):
+    """A load node away from mid-height (the benchmark's set draws it on the whole right edge):
     first design iteration against the oracle's direct solve."""
     nelx, nely, lj, vf, rm = 24, 12, 3, 0.45, 2.2
     b = tg.BatchedSIMP([nelx, 40], [nely, 20], [lj, 20], [vf, 0.5], [rm, 1.5], rtol=1e-10)
@@ -79,7 +79,7 @@ def test_batch_rejects_bad_problems(tg):
 def test_batch_tile_rows_same_results(tg, rows):
     """Every tile height gives the same design iteration on problems that span
     many tiles; compliance agrees to the solve tolerance."""
-    P = tg.config3_problems(8, seed=3)
+    P = tg.uneven_cantilever_set(8, seed=3)
     out = []
     for r in (rows, None):
         b = tg.BatchedSIMP(P["nelx"], P["nely"], P["load_j"], P["volfrac"], P["rmin"], rtol=1e-8)

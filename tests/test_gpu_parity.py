@@ -150,7 +150,7 @@ def test_oc_matches_oracle(tg, O):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32_ir"])
-def test_simp_config1_per_iteration(tg, O, precision):
+def test_simp_halfmbb_60x20_per_iteration(tg, O, precision):
     """HalfMBB 60x20, E_min 1e-9, p = 3, V = 0.5, rmin = 2, OC move 0.2, checked
     every design iteration on compliance (1e-6), sensitivities and filtered
     densities (1e-5) against the oracle's direct solve, for all 100 iterations

@@ -70,17 +70,17 @@ def test_host_argument_errors(tg):
     assert L.tog_destroy(None) == 0
 
 
-def test_config3_problem_set(tg):
+def test_uneven_cantilever_set(tg):
     """The batched benchmark's problem set: nelx even in [64, 512], nely = nelx / 2, load node
     on the right edge, volume fraction in [0.3, 0.6], rmin in [1.5, 3.0]; seeded."""
-    P = tg.config3_problems(256, seed=0)
+    P = tg.uneven_cantilever_set(256, seed=0)
     assert len(P["nelx"]) == 256
     assert np.all(P["nelx"] % 2 == 0) and P["nelx"].min() >= 64 and P["nelx"].max() <= 512
     assert np.all(P["nely"] * 2 == P["nelx"])
     assert np.all((P["load_j"] >= 0) & (P["load_j"] <= P["nely"]))
     assert P["volfrac"].min() >= 0.3 and P["volfrac"].max() <= 0.6
     assert P["rmin"].min() >= 1.5 and P["rmin"].max() <= 3.0
-    Q = tg.config3_problems(256, seed=0)
+    Q = tg.uneven_cantilever_set(256, seed=0)
     assert all(np.array_equal(P[k], Q[k]) for k in ("nelx", "nely", "load_j", "volfrac", "rmin"))
 
 

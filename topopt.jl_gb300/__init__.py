@@ -34,7 +34,6 @@ from .topopt_api import (  # noqa: F401
     VolumeFun,
     WarmStartNet,
     cell_dofs,
-    config3_problems,
     element_stiffness,
     find_nearest_dofs,
     generate_scenarios,
@@ -48,4 +47,5 @@ from .topopt_api import (  # noqa: F401
     mma_reset,
     mma_update,
     oc_update,
+    uneven_cantilever_set,
 )

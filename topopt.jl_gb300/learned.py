@@ -7,7 +7,7 @@ correction d of the previous displacement; the exact correction is K^-1 r0, so
 the network learns an approximate inverse of K(rho) applied to the residual.  The solver moves u_prev along d by the Galerkin step
 alpha = d.r0 / d.K d before its PCG solve, so a poor prediction can never make
 the start worse in the energy norm, and every solve still finishes to the same
-residual tolerance: plain PCG stays both the fallback and the judge.
+residual tolerance: plain PCG stays both the fallback and the measure of the result.
 
 Training data are the solver's own trajectories: seeded cantilever runs with
 random volume fraction, load node on the free face and load direction

@@ -828,8 +828,8 @@ class SIMPLoop:
 
 
 # --------------------------------------------------------------------------- batched 2D
-def config3_problems(n=256, seed=0):
-    """Problem set of the batched benchmark configuration: nelx ~ U{64..512} (even),
+def uneven_cantilever_set(n=256, seed=0):
+    """The seeded set of uneven 2D cantilevers of the batched benchmark: nelx ~ U{64..512} (even),
     nely = nelx / 2, the load node uniform on the right edge, volume fraction
     ~ U[0.3, 0.6], rmin ~ U[1.5, 3.0], from numpy default_rng(seed)."""
     rng = np.random.default_rng(seed)
