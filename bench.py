@@ -490,6 +490,77 @@ def run_profile(args):
     return 0
 
 
+def run_rows(args):
+    """Timings of the entry points beside the headline loop at 160x80x80 (FP32-IR unless
+    stated; host wall time around each call after a CUDA synchronize, so the host-array
+    calls include their copies): a design iteration of the device SIMP loop with OC and with
+    MMA (3 timed after 3 warm-up each), the MMA update and the fixed-element projection /
+    pullback on their own, a 3-load mean compliance (three cold solves), and an FP64 solve
+    under the residual-norm rule and under EnergyCriteria.  Prints one JSON line."""
+    import time
+    import torch
+    import __graft_entry__ as ge
+    tg = ge.load()
+
+    def timed(fn, reps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            out = fn()
+        torch.cuda.synchronize()
+        return 1e3 * (time.perf_counter() - t0) / reps, out
+
+    prob = tg.PointLoadCantilever(NELS, (1.0,) * 3, load="face_centre")
+    n = prob.ncells
+    out = {"workload": "3D PointLoadCantilever %dx%dx%d, V %.1f, rmin %.1f, p %.0f" % (NELS + (VOLFRAC, RMIN, PEN))}
+    for opt in ("oc", "mma"):
+        s = tg.FEASolver(tg.GB300Solver, prob, xmin=XMIN, penalty=tg.PowerPenaltyFun(PEN), rtol=RTOL, abstol=0.0,
+                         cg_max_iter=200000, precision="fp32_ir", warm_start=True)
+        loop = tg.SIMPLoop(s, volfrac=VOLFRAC, rmin=RMIN, filter="density", optimizer=opt)
+        for _ in range(3):
+            loop.step()
+        ms, st = timed(loop.step, 3)
+        out["simp_iteration_ms_" + opt] = ms
+        out["simp_last_" + opt] = {"compliance": float(st.compliance), "volume": float(st.volume),
+                                   "cg_iterations": int(st.cg_iterations)}
+        s.close()
+    s = tg.FEASolver(tg.GB300Solver, prob, xmin=XMIN, penalty=tg.PowerPenaltyFun(PEN), rtol=RTOL, abstol=0.0,
+                     cg_max_iter=200000, precision="fp32_ir")
+    rng = np.random.default_rng(0)
+    x = rng.uniform(0.2, 0.8, n)
+    df0 = -rng.uniform(0.1, 1.0, n)
+    dg = np.full(n, 1.0 / n)
+    tg.mma_update(s, x, df0, float(np.mean(x)) - VOLFRAC, dg)
+    out["mma_update_ms_host_arrays"], _ = timed(lambda: tg.mma_update(s, x, df0, float(np.mean(x)) - VOLFRAC, dg), 5)
+    black = [e for e in range(n) if e % NELS[0] == 0]
+    g = tg.get_fixed_element_projector(s, black, [])
+    xf = np.full(tg.get_free_variable_count(g), 0.5)
+    g(xf)
+    out["fixed_project_ms_host_arrays"], _ = timed(lambda: g(xf), 5)
+    out["fixed_pullback_ms_host_arrays"], _ = timed(lambda: g.pullback(x), 5)
+    g.detach()
+    rules = [((NELS[0], NELS[1] / 2, NELS[2] / 2), lambda: np.array([0.0, -1.0, 0.0])),
+             ((NELS[0], NELS[1], NELS[2] / 2), lambda: np.array([0.0, 0.0, 1.0])),
+             ((NELS[0] / 2, NELS[1], NELS[2]), lambda: np.array([1.0, 0.0, 0.0]))]
+    ml = tg.MultiLoad(prob, 1, rules[:1])
+    import scipy.sparse as sp
+    ml.F = sp.hstack([tg.MultiLoad(prob, 1, [r]).F for r in rules]).tocsc()
+    mc = tg.MeanComplianceFun(ml, s, method="exact")
+    xs = np.full(n, VOLFRAC)
+    out["mean_compliance_3_loads_ms"], c = timed(lambda: mc(tg.PseudoDensities(xs)), 1)
+    out["mean_compliance_3_loads_pcg_iterations"] = int(mc._ml.last_stats.iterations)
+    s.close()
+    for name, conv in (("default", tg.DefaultCriteria()), ("energy", tg.EnergyCriteria())):
+        s = tg.FEASolver(tg.GB300Solver, prob, xmin=XMIN, penalty=tg.PowerPenaltyFun(PEN), rtol=RTOL, abstol=0.0,
+                         cg_max_iter=200000, precision="fp64", conv=conv)
+        s.vars = xs
+        ms, _ = timed(s, 1)
+        out["fp64_solve_" + name] = {"ms": ms, "iterations": int(s.last_stats.iterations)}
+        s.close()
+    print(json.dumps(out))
+    return 0
+
+
 def run_profile_batch(args):
     """Profiling driver of the batched 2D operator: the benchmark's 256 uneven cantilevers,
     the band height pinned to args.profile_batch rows, five launches of the FP32 operator
@@ -516,6 +587,7 @@ def main():
     ap.add_argument("--no-extra", action="store_true", help="skip the e2e, accuracy, FP64 and roofline legs")
     ap.add_argument("--profile", action="store_true", help="run the small ncu driver instead of the benchmark")
     ap.add_argument("--nels", default="256,128,128", help="grid of --profile")
+    ap.add_argument("--rows", action="store_true", help="time the entry points beside the headline loop")
     ap.add_argument("--profile-batch", type=int, default=0, metavar="ROWS",
                     help="run the batched-operator ncu driver with this band height instead of the benchmark")
     args = ap.parse_args()
@@ -523,6 +595,8 @@ def main():
         return run_profile(args)
     if args.profile_batch:
         return run_profile_batch(args)
+    if args.rows:
+        return run_rows(args)
     if args.warmup < 3:
         log("warmup raised to 3 (timing rule)")
         args.warmup = 3
