@@ -163,7 +163,7 @@ end
 # ---- multiple loads: MeanComplianceFun / BlockComplianceFun (src/Functions/mean_compliance.jl,
 #      block_compliance.jl) on a GB300FEASolver.  The reference's versions need the per-element
 #      Kes the GB300 solver never builds; these methods solve every rhs column on the device.
-const TF = TopOpt.Functions
+const TOF = TopOpt.Functions
 function _multiload!(s::GB300FEASolver, cols::SparseMatrixCSC)
     length(s.vars) == getncells(s.problem) || throw(DimensionMismatch("vars"))
     check(ccall((:tog_set_vars, libtog), Cint, (Ptr{Cvoid}, Ptr{Float64}), s.handle, s.vars))
@@ -183,17 +183,17 @@ function _multiload_grad!(out, s::GB300FEASolver, w::AbstractVector)
                 s.handle, Int32(length(w)), Vector{Float64}(w), out))
     return out
 end
-_ml_columns(m::TF.ExactMean, F) = (sparse(F), size(F, 2))
-_ml_columns(m::TF.ExactSVDMean, F) = (sparse(m.US), m.n)
-function _ml_columns(m::TF.TraceEstimationMean, F)
+_ml_columns(m::TOF.ExactMean, F) = (sparse(F), size(F, 2))
+_ml_columns(m::TOF.ExactSVDMean, F) = (sparse(m.US), m.n)
+function _ml_columns(m::TOF.TraceEstimationMean, F)
     m.sample_once || m.sample_method(m.V)
     return sparse(m.F * m.V), size(m.V, 2) * size(m.F, 2)
 end
-function _ml_columns(m::TF.TraceEstimationSVDMean, F)
+function _ml_columns(m::TOF.TraceEstimationSVDMean, F)
     m.sample_once || m.sample_method(m.V)
     return sparse(m.US * m.V), size(m.V, 2) * m.n
 end
-function (ec::TF.MeanComplianceFun{T,<:ComplianceFun{T,<:GB300FEASolver}})(x::PseudoDensities) where {T}
+function (ec::TOF.MeanComplianceFun{T,<:ComplianceFun{T,<:GB300FEASolver}})(x::PseudoDensities) where {T}
     s = ec.compliance.solver
     s.vars .= x.x
     cols, n = _ml_columns(ec.method, ec.F)
@@ -201,13 +201,13 @@ function (ec::TF.MeanComplianceFun{T,<:ComplianceFun{T,<:GB300FEASolver}})(x::Ps
     _multiload_grad!(ec.grad, s, fill(1.0 / n, size(cols, 2)))
     return sum(c) / n
 end
-function TF.compute_block_compliance(bc::TF.BlockComplianceFun{T,<:ComplianceFun{T,<:GB300FEASolver}},
-                                     m::TF.ExactDiagonal) where {T}
+function TOF.compute_block_compliance(bc::TOF.BlockComplianceFun{T,<:ComplianceFun{T,<:GB300FEASolver}},
+                                     m::TOF.ExactDiagonal) where {T}
     bc.raw_val .= _multiload!(bc.compliance.solver, sparse(m.F))
     return bc.raw_val
 end
-function TF.compute_jtvp!_bc(out, bc::TF.BlockComplianceFun{T,<:ComplianceFun{T,<:GB300FEASolver}},
-                             m::TF.ExactDiagonal, w) where {T}
+function TOF.compute_jtvp!_bc(out, bc::TOF.BlockComplianceFun{T,<:ComplianceFun{T,<:GB300FEASolver}},
+                             m::TOF.ExactDiagonal, w) where {T}
     return _multiload_grad!(out, bc.compliance.solver, w)
 end
 
@@ -308,7 +308,7 @@ struct GB300ProjectedDensityFilter{TF<:GB300DensityFilter,TP1,TP2} <: AbstractDe
 end
 function TopOpt.CheqFilters.ProjectedDensityFilterFun(s::GB300FEASolver; rmin,
                                                       projection=TopOpt.Utilities.HeavisideProjectionFun(10.0))
-    return GB300ProjectedDensityFilter(DensityFilterFun(s, rmin), nothing, projection)
+    return GB300ProjectedDensityFilter(TopOpt.CheqFilters.DensityFilterFun(s, rmin), nothing, projection)
 end
 function _projected_forward(f::GB300ProjectedDensityFilter, x::AbstractVector)
     s = f.filter.solver
@@ -405,10 +405,12 @@ end
 IterStats() = IterStats(0, 0, 0, 0, 0, 0, 0, 0, 0)
 
 """
-    simp_init!(solver, x0; volfrac, rmin, filter=:density, move=0.2)
+    simp_init!(solver, x0; volfrac, rmin, filter=:density, move=nothing, optimizer=:oc)
     simp_step!(solver) -> IterStats
 
 Device-resident SIMP loop: one call per design iteration, the design stays in HBM.
+`optimizer` is `:oc` (move limit 0.2 unless `move` is given) or `:mma` (the volume
+constraint through MMA, move limit 0.5 unless given).
 """
 function simp_init!(s::GB300FEASolver, x0::AbstractVector; volfrac, rmin=0.0, filter=:density, move=nothing,
                     optimizer=:oc)
