@@ -138,6 +138,13 @@ int tog_matvec(tog_handle* h, const double* x, double* y);
  * current u (previous solve or tog_set_u) instead of 0. */
 int tog_solve(tog_handle* h, int32_t precision, double rtol, double abstol, int32_t maxiter, int32_t warm_start,
               tog_solve_stats* stats);
+/* One iteration's operator kernel of the Jacobi PCG (the inner loop of cg!,
+ * solvers_api.jl:197-218, over MatrixFreeOperator mul!, matrix_free_operator.jl:66-105):
+ * p = D^-1 r + beta p_old, q = K(rho) p (prescribed rows: meandiag p) and p.q, run once
+ * on caller vectors (reference dof order) in TOG_FP64 or, for TOG_FP32_IR, in the FP32
+ * arithmetic of the refinement's inner PCG.  pq may be NULL. */
+int tog_pcg_operator(tog_handle* h, int32_t precision, double beta, const double* r, const double* p_old, double* p,
+                     double* q, double* pq);
 /* solver.u (reference dof order). */
 int tog_get_u(tog_handle* h, double* u);
 int tog_set_u(tog_handle* h, const double* u);
@@ -325,13 +332,16 @@ int tog_record_status(tog_handle* h, int32_t* written);
 /* ---- allocation-free OC update: no counterpart in TopOpt.jl ----------------------------
  * For callers that cannot call cudaMalloc (a framework that owns and pre-partitions all
  * device memory, a memory-capped service, a loop that must not allocate between
- * iterations).  Same update as tog_oc_update, on the caller's DEVICE arrays of n cells,
+ * iterations).  The update of tog_oc_update, on the caller's DEVICE arrays of n cells,
  * launched on `stream` (cudaStream_t as void*, may be NULL) without a host sync;
  * result_dev[0..2] = change, lambda, volume.  Allocates nothing: its scratch is a static
  * device array of the library (about 8.1 MiB on every GPU that loads it, held until exit),
  * so n must be <= 1,048,576 (TOG_ERR_ARG otherwise).  The first call on a device looks up
- * the array's address (make it before any stream capture).  Calls share the array; calls
- * that overlap on the GPU race. */
+ * the array's address (make it before any stream capture) and keeps it for the process,
+ * so do not call cudaDeviceReset between calls.  Calls share the array; calls that overlap
+ * on the GPU race.  Having no handle, it does not hold the cells of tog_set_fixed_elements:
+ * every cell is free (pass a design with fixed cells to tog_oc_update instead).  Its 100
+ * bisection launches are all issued; those after convergence return at once. */
 int tog_oc_update_noalloc(int64_t n, const double* x_dev, const double* dc_dev, const double* dv_dev,
                           const double* w_dev, double volfrac, double move, double* xnew_dev, double* result_dev,
                           void* stream);

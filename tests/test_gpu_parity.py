@@ -273,3 +273,54 @@ def test_projected_density_filter_matches_oracle(tg, O, nels, kind):
     with pytest.raises(tg.TopOptError):
         tg.ProjectedDensityFilterFun(s, rmin=rmin, projection=tg.HeavisideProjectionFun(-1.0))(x)
     s.close()
+
+
+@pytest.mark.parametrize("nels,kind", [((2, 2, 2), "cant"), ((7, 4, 6), "cant"), ((33, 9, 7), "mbb"),
+                                       ((61, 14, 6), "cant"), ((29, 30, 2), "cant"), ((40, 16, 18), "cant"),
+                                       ((96, 48, 48), "cant")])
+def test_fp32_pcg_operator_matches_oracle(tg, O, nels, kind):
+    """The FP32 PCG operator kernel (the inner loop of cg!, solvers_api.jl:197-218, over
+    MatrixFreeOperator mul!, matrix_free_operator.jl:66-105) on one launch:
+    p = D^-1 r + beta p_old and q = K p against the oracle in FP64, across x strips
+    and z bands that end inside the grid.  FP32 inputs and arithmetic: 2e-6 relative
+    to max |q|, p within FP32 rounding (1e-6); p.q 1e-5."""
+    p, op = make(tg, O, nels, kind)
+    s = tg.FEASolver(tg.GB300Solver, p, xmin=1e-3, penalty=tg.PowerPenaltyFun(3.0))
+    rng = np.random.default_rng(11)
+    s.vars = rng.uniform(0.05, 1.0, p.ncells)
+    st = O.fea_setup(op, xmin=1e-3, p=3.0)
+    st.vars = s.vars
+    r = rng.standard_normal(p.ndofs)
+    pold = rng.standard_normal(p.ndofs)
+    r[~st.free_mask] = 0.0      # as in the PCG: prescribed residuals and directions stay zero
+    pold[~st.free_mask] = 0.0
+    beta = 0.37
+    pg, qg, pq = s.pcg_operator(r, pold, beta, precision="fp32_ir")
+    pr = r / O.jacobi_diag(st) + beta * pold
+    qr = O.matvec(st, pr)
+    assert rel(pg, pr) < 1e-6
+    assert rel(qg, qr) < 2e-6
+    assert abs(pq - pr @ qr) <= 1e-5 * abs(pr @ qr)
+    s.close()
+
+
+@pytest.mark.parametrize("nels,kind", [((7, 4, 6), "cant"), ((40, 16, 18), "cant"), ((60, 20), "mbb")])
+def test_fp64_pcg_operator_matches_oracle(tg, O, nels, kind):
+    """The FP64 PCG operator (tile kernel and tile-boundary gather in 3D) on one launch: 1e-12."""
+    p, op = make(tg, O, nels, kind)
+    s = tg.FEASolver(tg.GB300Solver, p, xmin=1e-3, penalty=tg.PowerPenaltyFun(3.0))
+    rng = np.random.default_rng(12)
+    s.vars = rng.uniform(0.05, 1.0, p.ncells)
+    st = O.fea_setup(op, xmin=1e-3, p=3.0)
+    st.vars = s.vars
+    r = rng.standard_normal(p.ndofs)
+    pold = rng.standard_normal(p.ndofs)
+    r[~st.free_mask] = 0.0
+    pold[~st.free_mask] = 0.0
+    pg, qg, pq = s.pcg_operator(r, pold, -0.25, precision="fp64")
+    pr = r / O.jacobi_diag(st) - 0.25 * pold
+    qr = O.matvec(st, pr)
+    assert rel(pg, pr) < 1e-14
+    assert rel(qg, qr) < 1e-12
+    assert abs(pq - pr @ qr) <= 1e-12 * abs(pr @ qr)
+    s.close()

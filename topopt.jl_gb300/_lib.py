@@ -62,6 +62,7 @@ SIGNATURES = {
     "tog_set_penalty": (C.c_int, [_H, C.c_double]),
     "tog_set_vars": (C.c_int, [_H, _D]),
     "tog_matvec": (C.c_int, [_H, _D, _D]),
+    "tog_pcg_operator": (C.c_int, [_H, C.c_int32, C.c_double, _D, _D, _D, _D, _D]),
     "tog_solve": (C.c_int, [_H, C.c_int32, C.c_double, C.c_double, C.c_int32, C.c_int32, C.POINTER(SolveStats)]),
     "tog_get_u": (C.c_int, [_H, _D]),
     "tog_set_u": (C.c_int, [_H, _D]),

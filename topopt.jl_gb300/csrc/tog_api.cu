@@ -16,7 +16,6 @@
 #include "tog_nn.h"
 #include "tog_kernels.cuh"
 #include "tog_mv3.cuh"
-#include "tog_mv3x2.cuh"
 #include "tog_march3.cuh"
 #include "tog_mma.cuh"
 
@@ -151,13 +150,9 @@ struct tog_handle {
     // 3D operator tiling: tiles of 32 x MV3_BY elements, LZ layers per z chunk
     int nt[3] = {1, 1, 1};
     int LZ = 8;
-    bool mv3_scalar = true;    // FP32 tile operator: k_mv3 (scalar) unless TOG_MV3_KERNEL=pair
-    bool mv3_march = true;     // FP32 PCG operator: k_march3 unless TOG_MV3_KERNEL=tile / pair
-    int march_grid = 0;        // persistent grid of k_march3
+    int march_grid = 0;        // persistent grid of k_march3 (the 3D FP32 PCG operator)
     int march_nband = 1, march_lzb = 1;   // its z bands per node column and their height
-    double ru_delta = 0.03;    // FP32-IR reliable-update trigger: residual reduction factor (TOG_RU_DELTA;
-                               // 0.2 / 0.1 / 0.05 / 0.02 measured 12.6 / 12.9 / 13.1 / 13.3 design iters/s)
-    float* d_side32[8] = {};
+    double ru_delta = 0.03;    // FP32-IR reliable-update trigger: residual reduction factor (TOG_RU_DELTA)
     double* d_side64[8] = {};
     // graphs
     cudaGraphExec_t g_pcg64 = nullptr, g_pcg32 = nullptr, g_oc = nullptr;
@@ -312,13 +307,8 @@ Mv3Args<T> mv3_args(tog_handle* h) {
     A.div_nny = make_fastdiv((unsigned)h->nn[1]);
     A.div_nnz = make_fastdiv((unsigned)h->nn[2]);
     for (int c = 0; c < 8; ++c)
-        A.side[c] = std::is_same<T, double>::value ? (T*)h->d_side64[c] : (T*)h->d_side32[c];
+        A.side[c] = std::is_same<T, double>::value ? (T*)h->d_side64[c] : nullptr;   // FP64 tile operator only
     return A;
-}
-
-template <int MODE>
-void launch_mv3x2(tog_handle* h, cudaStream_t s, const Mv3Args<float>& A) {
-    k_mv3x2<MODE><<<dim3(h->nt[0], h->nt[1], h->nt[2]), dim3(32, MX_WARPS), 0, s>>>(A);
 }
 
 template <typename T, int MODE>
@@ -340,14 +330,15 @@ void launch_matvec(tog_handle* h, cudaStream_t s, const T* x, T* y, const double
         Mv3Args<T> A = mv3_args<T>(h);
         A.x = x;
         if (MODE == MV_RESID) A.st = h->d_st64;
-        if (std::is_same<T, float>::value && MODE == MV_PCG && h->mv3_march)
+        if constexpr (std::is_same<T, float>::value) {
+            // FP32 is used by the PCG of the refinement only: the warp march
+            static_assert(MODE == MV_PCG, "the 3D FP32 operator exists in PCG form only");
             k_march3<<<h->march_grid, 32 * kM3Warps, 0, s>>>(*reinterpret_cast<const Mv3Args<float>*>(&A),
                                                             (h->nn[0] + 29) / 30, h->march_nband, h->march_lzb);
-        else if (std::is_same<T, float>::value && MODE != MV_RESID && !h->mv3_scalar)
-            launch_mv3x2<MODE == MV_RESID ? MV_PLAIN : MODE>(h, s, *reinterpret_cast<const Mv3Args<float>*>(&A));
-        else
+        } else {
             launch_mv3<T, MODE>(h, s, A);
-        if (MODE != MV_PCG) {
+        }
+        if constexpr (MODE != MV_PCG) {
             k_mv3_finalize<T, MODE><<<h->ew_blocks(h->nnodes), kEwThreads, 0, s>>>(A, x, y, f, (T)h->meandiag);
             TOG_LAUNCHED(1);
         }
@@ -374,7 +365,7 @@ void launch_pcg_update(tog_handle* h, cudaStream_t s) {
                                  (long long)(h->nt[1] - 1) * h->nn[0] * h->nn[2] +
                                  (long long)(h->nt[2] - 1) * h->nn[0] * h->nn[1];
         // the FP32 march writes complete q: no tile-boundary partials to gather
-        const bool march = std::is_same<T, float>::value && h->mv3_march;
+        const bool march = std::is_same<T, float>::value;
         if (n_side > 0 && !march) {
             const long long nbs = std::min<long long>((n_side + kEwThreads - 1) / kEwThreads, (long long)h->nsm * 8);
             k_side_gather3<T><<<(int)nbs, kEwThreads, 0, s>>>(A);
@@ -1119,10 +1110,6 @@ int tog_create(const tog_problem_desc* desc, tog_handle** out) {
         h->nt[0] = (h->nel[0] + 31) / 32;
         h->nt[1] = (h->nel[1] + MV3_BY - 1) / MV3_BY;
         const long long txy = (long long)h->nt[0] * h->nt[1];
-        if (const char* e = std::getenv("TOG_MV3_KERNEL")) {
-            h->mv3_scalar = std::string(e) != "pair";
-            h->mv3_march = std::string(e) == "march";
-        }
         int bps = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_march3, 32 * kM3Warps, 0) != cudaSuccess || bps < 1)
             bps = 1;
@@ -1144,14 +1131,11 @@ int tog_create(const tog_problem_desc* desc, tog_handle** out) {
         }
         int occ = 0;
         cudaError_t oe;
-        if (h->mv3_scalar) {
-            cudaFuncSetAttribute(k_mv3<float, MV_PCG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)sizeof(Mv3Smem<float>));
-            oe = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_mv3<float, MV_PCG>, 32 * MV3_BY,
-                                                               sizeof(Mv3Smem<float>));
-        } else {
-            oe = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_mv3x2<MV_PCG>, 32 * MX_WARPS, 0);
-        }
+        // z chunks of the FP64 tile operator (k_mv3<double>: FP64 PCG, true residual, K x)
+        cudaFuncSetAttribute(k_mv3<double, MV_PCG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)sizeof(Mv3Smem<double>));
+        oe = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_mv3<double, MV_PCG>, 32 * MV3_BY,
+                                                           sizeof(Mv3Smem<double>));
         if (oe != cudaSuccess || occ < 1) occ = 1;
         const long long slots = (long long)h->nsm * occ;
         int best = h->nel[2];
@@ -1226,7 +1210,6 @@ int tog_create(const tog_problem_desc* desc, tog_handle** out) {
     if (dim == 3)
         for (int c = 1; c < 8; ++c) {
             const long long cnt = 3 * std::max(1LL, side_count(c, h->nn, h->nt));
-            A(dalloc(&h->d_side32[c], cnt));
             A(dalloc(&h->d_side64[c], cnt));
         }
     if (rc == TOG_OK) {
@@ -1290,7 +1273,6 @@ int tog_destroy(tog_handle* h) {
     for (int i = 0; i < 6; ++i)
         if (h->d_cell[i]) cudaFree(h->d_cell[i]);
     for (int c = 0; c < 8; ++c) {
-        if (h->d_side32[c]) cudaFree(h->d_side32[c]);
         if (h->d_side64[c]) cudaFree(h->d_side64[c]);
     }
     if (h->h_st) cudaFreeHost(h->h_st);
@@ -1379,6 +1361,59 @@ int tog_matvec(tog_handle* h, const double* x, double* y) {
     launch_matvec<double, MV_PLAIN>(h, h->stream, h->d_p64[0], h->d_r64, nullptr);
     TOG_CUDA(cudaGetLastError());
     return download_dofs(h, h->d_r64, y);
+}
+
+// One fused PCG operator launch on caller vectors (the kernel every PCG iteration
+// runs first): p = D^-1 r + beta p_old, q = K(rho) p with the prescribed rows set
+// to meandiag p (as the PCG update uses it), p.q.
+int tog_pcg_operator(tog_handle* h, int32_t precision, double beta, const double* r, const double* p_old, double* p,
+                     double* q, double* pq) {
+    TOG_TRY(check_handle(h));
+    if (!r || !p_old || !p || !q) return fail(TOG_ERR_ARG, "null vector");
+    if (precision != TOG_FP64 && precision != TOG_FP32_IR) return fail(TOG_ERR_ARG, "bad precision");
+    if (!std::isfinite(beta)) return fail(TOG_ERR_ARG, "beta must be finite");
+    TOG_TRY(refresh_scales(h));
+    const bool f32 = precision == TOG_FP32_IR;
+    const long long nd = h->ndofs;
+    const int nb = h->ew_blocks(nd);
+    PcgState* d_st = f32 ? h->d_st32 : h->d_st64;
+    if (f32) {
+        TOG_TRY(upload_dofs(h, r, h->d_tmp));
+        k_cast_f32<<<nb, kEwThreads, 0, h->stream>>>(h->d_tmp, h->d_r32, nd);
+        TOG_TRY(upload_dofs(h, p_old, h->d_tmp));
+        k_cast_f32<<<nb, kEwThreads, 0, h->stream>>>(h->d_tmp, h->d_p32[1], nd);
+        TOG_LAUNCHED(2);
+    } else {
+        TOG_TRY(upload_dofs(h, r, h->d_r64));
+        TOG_TRY(upload_dofs(h, p_old, h->d_p64[1]));
+    }
+    // iteration 0 (direction into P0, previous direction from P1), r.z = 1
+    PcgState* hs = h->h_st;
+    std::memset(hs, 0, sizeof(PcgState));
+    hs->rz = 1.0;
+    hs->beta = beta;
+    hs->maxit = 1 << 30;
+    TOG_CUDA(cudaMemcpyAsync(d_st, hs, sizeof(PcgState), cudaMemcpyHostToDevice, h->stream));
+    if (f32) {
+        launch_matvec<float, MV_PCG>(h, h->stream, nullptr, nullptr, nullptr);
+        k_pcg_operator_out<float><<<h->ew_blocks(h->nnodes), kEwThreads, 0, h->stream>>>(
+            h->d_p32[0], h->d_q32, h->d_fixmask, h->meandiag, h->nnodes, h->dim, h->d_tmp, h->d_r64);
+    } else {
+        launch_matvec<double, MV_PCG>(h, h->stream, nullptr, nullptr, nullptr);
+        if (h->dim == 3) {   // the tile operator leaves tile-boundary partials for the PCG update to gather
+            Mv3Args<double> A = mv3_args<double>(h);
+            k_side_gather3<double><<<h->ew_blocks(h->nnodes), kEwThreads, 0, h->stream>>>(A);
+            TOG_LAUNCHED(1);
+        }
+        k_pcg_operator_out<double><<<h->ew_blocks(h->nnodes), kEwThreads, 0, h->stream>>>(
+            h->d_p64[0], h->d_q64, h->d_fixmask, h->meandiag, h->nnodes, h->dim, h->d_tmp, h->d_r64);
+    }
+    TOG_LAUNCHED(1);
+    TOG_CUDA(cudaGetLastError());
+    TOG_TRY(sync_state(h, d_st));
+    if (pq) *pq = h->h_st->pq;
+    TOG_TRY(download_dofs(h, h->d_tmp, p));
+    return download_dofs(h, h->d_r64, q);
 }
 
 int tog_solve(tog_handle* h, int32_t precision, double rtol, double abstol, int32_t maxiter, int32_t warm_start,
@@ -1968,7 +2003,7 @@ int tog_kernel_bytes(tog_handle* h, int32_t kernel, int32_t precision, double* b
     if (!bytes || kernel < 0 || kernel > 1) return fail(TOG_ERR_ARG, "bad kernel id or null output");
     const double s = precision == TOG_FP64 ? 8.0 : 4.0;
     const double N = (double)h->ndofs, Nn = (double)h->nnodes, E = (double)h->ncells;
-    const bool march = h->dim == 3 && precision != TOG_FP64 && h->mv3_march;
+    const bool march = h->dim == 3 && precision != TOG_FP64;
     if (kernel == 0)   // reads r, p_old, D^-1, E_e (and the fixed mask, except the 3D march); writes p, q
         *bytes = 4.0 * s * N + s * Nn + s * E + (march ? 0.0 : Nn);
     else               // reads q, p, x, r, D^-1, mask; writes x, r

@@ -868,6 +868,33 @@ __global__ void __launch_bounds__(256) k_fixed_pin(double* __restrict__ x, const
     }
 }
 
+// FP64 -> FP32 copy of a dof vector
+__global__ void __launch_bounds__(256) k_cast_f32(const double* __restrict__ src, float* __restrict__ dst,
+                                                  long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        dst[i] = (float)src[i];
+}
+
+// Output of one PCG operator launch in FP64: p, and q with the prescribed rows
+// replaced by meandiag p (what the PCG update does with them)
+template <typename T>
+__global__ void __launch_bounds__(256) k_pcg_operator_out(const T* __restrict__ p, const T* __restrict__ q,
+                                                          const uint8_t* __restrict__ fixmask, double meandiag,
+                                                          long long nnodes, int dim, double* __restrict__ pout,
+                                                          double* __restrict__ qout) {
+    for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < nnodes;
+         n += (long long)gridDim.x * blockDim.x) {
+        const unsigned m = fixmask[n];
+        for (int c = 0; c < dim; ++c) {
+            const long long i = dim * n + c;
+            const double pv = (double)p[i];
+            pout[i] = pv;
+            qout[i] = ((m >> c) & 1u) ? meandiag * pv : (double)q[i];
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // dof permutation between the reference (Ferrite) order and the internal order
 // ---------------------------------------------------------------------------

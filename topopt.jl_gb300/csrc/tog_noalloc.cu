@@ -3,10 +3,11 @@
 // Some callers cannot call cudaMalloc: a host framework that owns and
 // pre-partitions all device memory, a memory-capped service, or a caller whose
 // optimisation loop must not allocate between iterations.  This entry point
-// runs the same optimality-criteria bisection as tog_oc_update on device arrays
-// the caller passes in, and keeps its only scratch -- the per-element OC
-// factors, the block partial sums and the bisection state -- in one static
-// __device__ array of this file.
+// runs the optimality-criteria bisection of tog_oc_update on device arrays the
+// caller passes in, and keeps its only scratch -- the per-element OC factors,
+// the block partial sums and the bisection state -- in one static __device__
+// array of this file.  It has no handle, so every cell is free: the fixed
+// (black / white) cells of tog_set_fixed_elements are not held here.
 //
 // Limits and rules of use:
 //   * at most kNoallocMaxCells cells (8 MiB of factors); larger n is rejected.
@@ -14,7 +15,10 @@
 //     the process exits.
 //   * the first call on a device looks up the array's device address with
 //     cudaGetSymbolAddress (once per device, that device current); make that
-//     first call before any stream capture.
+//     first call before any stream capture.  The address is kept for the
+//     process: a cudaDeviceReset between calls would leave it stale.
+//   * the 100 bisection launches are always issued (no host synchronisation);
+//     the ones after convergence return at once.
 //   * all calls share the array and it keeps the last call's contents; each
 //     call re-initialises the bisection state and counters it relies on.
 //     Calls that overlap on the GPU (different streams, or threads) race on it.

@@ -283,6 +283,20 @@ class GB300FEASolver:
         L.check(L.lib().tog_matvec(self.handle, L.dptr(x), L.dptr(y)))
         return y
 
+    def pcg_operator(self, r, p_old, beta, precision="fp32_ir"):
+        """One launch of the PCG's fused operator kernel at the current vars:
+        p = D^-1 r + beta p_old and q = K p (prescribed rows meandiag p), p.q
+        (the inner loop of cg!, solvers_api.jl:197-218)."""
+        self._push_vars()
+        r = np.ascontiguousarray(r, dtype=np.float64)
+        p_old = np.ascontiguousarray(p_old, dtype=np.float64)
+        p, q = np.empty_like(r), np.empty_like(r)
+        pq = L.C.c_double()
+        prec = L.TOG_FP64 if precision == "fp64" else L.TOG_FP32_IR
+        L.check(L.lib().tog_pcg_operator(self.handle, prec, float(beta), L.dptr(r), L.dptr(p_old), L.dptr(p),
+                                         L.dptr(q), L.C.byref(pq)))
+        return p, q, pq.value
+
 
 def FEASolver(solver_type, problem, **kw):
     if solver_type is not GB300Solver:
