@@ -26,13 +26,16 @@ sys.path.insert(0, ROOT)
 METRIC = "design iters/s, 3D hex8 1M elems: learned+FP32-IR vs plain FP64 PCG @ rel 1e-6"
 NELS = (160, 80, 80)
 VOLFRAC, RMIN, PEN, XMIN, RTOL, MOVE = 0.3, 1.5, 3.0, 1e-9, 1e-8, 0.2
-WORKLOAD = ("3D PointLoadCantilever 160x80x80 hex8 (1,024,000 elements, 3,168,963 dofs), E0=1, nu=0.3, "
-            "E_min=1e-9, unit load at the right-face centre, SIMP p=3, V=0.3, density filter rmin=1.5, "
-            "x0=0.3, OC move 0.2, solve rtol 1e-8")
-# FP64 Jacobi-PCG iterations per design iteration on this workload (cold start,
-# rtol 1e-8), measured by this script's FP64 leg on a GB300; the CPU reference
-# arm multiplies its measured per-iteration time by it.
-REF_CG_ITERS_DEFAULT = 1000
+WORKLOAD = ("3D PointLoadCantilever 160x80x80 hex8, 1,024,000 cells, E_min 1e-9, load at right-face centre, "
+            "p=3, V=0.3, rmin=1.5, x0=0.3, OC move 0.2, rtol 1e-8")
+# seconds of CPU design iterations the reference arm times at most (whole iterations only)
+REF_BUDGET_S = float(os.environ.get("REF_BUDGET_S", "150"))
+
+
+def config_line():
+    """The `config` object both arms print (short values: it is compared between the arms)."""
+    return {"workload": WORKLOAD, "unit_of_work": "one design iteration (filter, solve, compliance, pullback, OC)",
+            "l2": "working set ~0.3 GB > 129 MB L2 (no flush)"}
 
 
 def log(*a):
@@ -130,64 +133,73 @@ def barrier(ws):
 
 
 # --------------------------------------------------------------------------- CPU legs
-def cpu_sample(threads, cg_iters, sample_iters):
-    """Time the oracle port of the reference path on the host: one full set of the
-    non-solve work (filter, compliance, filter pullback, OC) plus `sample_iters`
-    Jacobi-PCG iterations; scale the PCG part to `cg_iters` iterations per design
-    iteration."""
+def cpu_design_iterations(threads, max_iters, budget_s):
+    """The oracle port of the reference path (per-element Ke copies, two-phase gather,
+    Jacobi PCG from zero to rtol on the recurrence residual as cg!, compliance, filter
+    pullback, OC) run as whole design iterations from the uniform start on `threads`
+    host threads, each one timed; stops after `max_iters` or once `budget_s` seconds of
+    iterations have run.  Returns the per-iteration seconds and PCG counts, and the
+    first iteration's filtered densities, displacement, compliance, sensitivities and
+    new design (the accuracy reference of the GPU path)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import topopt_oracle as O
     import oracle_cpu as OC
     prob = O.point_load_cantilever(NELS, (1.0, 1.0, 1.0), load="face_centre")
     Ke = O.element_stiffness(3, (1.0, 1.0, 1.0), 1.0, 0.3)
-    t0 = time.perf_counter()
     cs = OC.CPUSolver(prob, Ke, XMIN, PEN, threads=threads)
-    t_setup = time.perf_counter() - t0
     n = prob.grid.ncells
-    x = np.full(n, VOLFRAC)
     cs.filter_setup(RMIN)
-    t0 = time.perf_counter()
-    xf = cs.filter_J(x)
-    cs.set_vars(xf)
-    t_a = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    u, it, _ = cs.pcg(prob.f, rtol=0.0, abstol=0.0, maxit=sample_iters)
-    t_pcg = (time.perf_counter() - t0) / max(it, 1)
-    t0 = time.perf_counter()
-    c, g = cs.compliance(u)
-    dc = cs.filter_JT(g)
-    dv = cs.filter_JT(np.full(n, 1.0 / n))
-    cs.oc(x, dc, dv, dv, VOLFRAC, MOVE)
-    t_b = time.perf_counter() - t0
+    f = prob.f.copy()
+    f[prob.fixed_dofs] = 0.0
+    x = np.full(n, VOLFRAC)
+    secs, cg, first = [], [], None
+    while len(secs) < max_iters and (not secs or sum(secs) < budget_s):
+        t0 = time.perf_counter()
+        xf = cs.filter_J(x)
+        cs.set_vars(xf)
+        u, it, _ = cs.pcg(f, rtol=RTOL, abstol=0.0, maxit=200000)
+        c, g = cs.compliance(u)
+        dc = cs.filter_JT(g)
+        dv = cs.filter_JT(np.full(n, 1.0 / n))
+        xn, _, _ = cs.oc(x, dc, dv, dv, VOLFRAC, MOVE)
+        secs.append(time.perf_counter() - t0)
+        cg.append(int(it))
+        if first is None:
+            first = dict(xf=xf, u=u, c=c, dc=dc, x_new=xn)
+        x = xn
     cs.close()
-    per_iter = t_a + t_b + cg_iters * t_pcg
-    return dict(seconds_per_design_iter=per_iter, seconds_per_pcg_iter=t_pcg, other_seconds=t_a + t_b,
-                setup_seconds=t_setup, sample_pcg_iters=it)
+    return dict(seconds=secs, cg_iters=cg, first=first, threads=threads)
+
+
+def cpu_threads():
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_cpu as OC
+    return OC.lib().orc_max_threads()
 
 
 def run_reference(args):
+    """The reference's CPU path (the oracle port, all host threads) timed over whole
+    design iterations of the same workload: as many as fit in REF_BUDGET_S seconds,
+    at most --steps; the line's steps is the number timed."""
     ws, rank, _ = dist_setup()
     if rank != 0:
         return 0
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle_cpu as OC
-    threads = OC.lib().orc_max_threads()
-    cg_iters = int(os.environ.get("REF_CG_ITERS", REF_CG_ITERS_DEFAULT))
-    per = []
-    for s in range(args.warmup + args.steps):
-        r = cpu_sample(threads, cg_iters, sample_iters=3)
-        if s >= args.warmup:
-            per.append(r["seconds_per_design_iter"])
-    v = len(per) / sum(per)
+    threads = cpu_threads()
+    r = cpu_design_iterations(threads, args.steps, REF_BUDGET_S)
+    k = len(r["seconds"])
+    t = sum(r["seconds"])
+    v = k / t
+    sample = ("design iterations 1..%d from the uniform start, each whole (filter, cold Jacobi PCG to rtol 1e-8: "
+              "%s iterations, compliance, pullback, OC), %d of the %d steps asked fit in %.0f s"
+              % (k, ",".join(map(str, r["cg_iters"])), k, args.steps, REF_BUDGET_S))
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "design_iters/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(per) / len(per),
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD},
+            "steps": k, "warmup": 0, "ms_per_step": 1e3 * t / k, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config_line(),
             "cpu_baseline": {"value": v, "unit": "design_iters/s", "cores": threads, "kind": "port",
-                             "sample": "per step: filter + compliance + filter pullback + OC once, 3 Jacobi-PCG "
-                                       "iterations timed and scaled to %d iterations per design iteration "
-                                       "(the FP64 PCG count of this workload)" % cg_iters},
-            "e2e": {"value": v, "unit": "design_iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+                             "sample": sample},
+            "e2e": {"value": v, "unit": "design_iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "steps_requested": args.steps, "warmup_requested": args.warmup,
+            "note": "CPU arm: no warm-up iteration (nothing to warm); whole design iterations only"}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -323,6 +335,7 @@ def run_ours(args):
     for _ in range(args.warmup):
         loop.step()
     torch.cuda.synchronize()
+    x_w, u_w = loop.x.copy(), solver.u.copy()   # the state the timed window starts from
     barrier(ws)
     l0 = L.lib().tog_launch_count()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -347,47 +360,37 @@ def run_ours(args):
                               "inner_cg_iters_per_step": [int(s.cg_iterations) for s in stats]}), flush=True)
         return 0
 
-    # ---- e2e: same loop through the C ABI with the design in pinned host memory
+    # ---- e2e: the same design iterations (restarted from the state after the warm-up)
+    #      through the C ABI, the design copied from and to pinned host memory every step
     xh = torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
-    xh[:] = loop.x
-    e_steps = max(2, min(args.steps, 5))
+    xh[:] = x_w
+    solver.u = u_w
     torch.cuda.synchronize()
     barrier(ws)
     f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e2e_cg = []
     with torch.cuda.stream(stream):
         f0.record(stream)
-        for _ in range(e_steps):
+        for _ in range(args.steps):
             L.check(L.lib().tog_set_design(solver.handle, L.dptr(xh)))
             st = L.IterStats()
             L.check(L.lib().tog_simp_step(solver.handle, L.TOG_FP32_IR, RTOL, 200000, 1, L.C.byref(st)))
             L.check(L.lib().tog_get_design(solver.handle, L.dptr(xh)))
+            e2e_cg.append(int(st.cg_iterations))
         f1.record(stream)
     torch.cuda.synchronize()
     t_e2e = max_over_ranks(f0.elapsed_time(f1) / 1e3, ws)
-    e2e = {"value": ws * e_steps / t_e2e, "unit": "design_iters/s", "h2d_bytes_per_step": 8 * n,
-           "d2h_bytes_per_step": 8 * n + 8}
+    e2e = {"value": ws * args.steps / t_e2e, "unit": "design_iters/s", "h2d_bytes_per_step": 8 * n,
+           "d2h_bytes_per_step": 8 * n + 8,
+           "window": "design iterations %d..%d, as value" % (args.warmup + 1, args.warmup + args.steps),
+           "cg_iters_mean": float(np.mean(e2e_cg))}
 
-    # ---- accuracy: FP32-IR vs FP64 PCG on the same filtered design
-    xphys = loop.physical
-    acc = {}
+    # ---- plain FP64 Jacobi PCG (cold start, as the reference) over the same design-iteration window
     s64 = make_solver("fp64", False)
-    comp64 = tg.ComplianceFun(s64)
-    c64 = comp64(tg.PseudoDensities(xphys))
-    it64 = s64.last_stats.iterations
-    comp32 = tg.ComplianceFun(solver)
-    solver.warm_start = False
-    c32 = comp32(tg.PseudoDensities(xphys))
-    solver.warm_start = True
-    acc = {"compliance_rel_err": abs(c32 - c64) / abs(c64),
-           "sens_rel_err": float(np.max(np.abs(comp32.grad - comp64.grad)) / np.max(np.abs(comp64.grad))),
-           "fp64_cg_iters": it64, "fp32ir_inner_iters_cold": solver.last_stats.iterations,
-           "fp32ir_outer_iters_cold": solver.last_stats.outer_iterations}
-
-    # ---- plain FP64 Jacobi PCG design iterations (cold start, as the reference)
     loop64 = tg.SIMPLoop(s64, volfrac=VOLFRAC, rmin=RMIN, filter="density")
-    k64 = max(1, min(args.steps, int(os.environ.get("FP64_STEPS", "2"))))
-    for _ in range(args.warmup):   # the same design-iteration indices as the timed FP32-IR steps
+    for _ in range(args.warmup):
         loop64.step(precision="fp64", warm_start=False)
+    k64 = max(1, min(args.steps, int(os.environ.get("FP64_STEPS", str(args.steps)))))
     g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     st64 = []
     torch.cuda.synchronize()
@@ -400,9 +403,28 @@ def run_ours(args):
     t64 = g0.elapsed_time(g1) / 1e3
     fp64 = {"value": k64 / t64, "unit": "design_iters/s", "steps": k64, "warmup": args.warmup,
             "cg_iters_per_step": [int(s.cg_iterations) for s in st64],
-            "note": "design iterations %d..%d of a cold-start FP64 trajectory (the FP32-IR leg times "
-                    "%d..%d)" % (args.warmup + 1, args.warmup + k64, args.warmup + 1, args.warmup + args.steps)}
+            "window": "design iterations %d..%d of a cold-start FP64 trajectory (FP32-IR: %d..%d)"
+                      % (args.warmup + 1, args.warmup + k64, args.warmup + 1, args.warmup + args.steps)}
+    fp64["fp32ir_vs_fp64"] = value / fp64["value"]
+    fp64["ms_per_pcg_iter_fp64"] = 1e3 * t64 / max(1, sum(fp64["cg_iters_per_step"]))
+    fp64["ms_per_pcg_iter_fp32ir"] = 1e3 * t_dev / max(1, sum(int(s.cg_iterations) for s in stats))
+
+    # ---- design iteration 1 on the GPU (FP32-IR and FP64), for the comparison with the oracle
     s64.close()
+    x0 = np.full(n, VOLFRAC)
+    first = {}
+    for name in ("fp32_ir", "fp64"):
+        s_ = make_solver(name, False)
+        df_ = tg.DensityFilterFun(s_, RMIN)
+        xf = df_(tg.PseudoDensities(x0)).x
+        comp = tg.ComplianceFun(s_)
+        c = comp(tg.PseudoDensities(xf))
+        g = comp.pullback(1.0)
+        dc = df_.pullback(g)
+        dv = df_.pullback(np.full(n, 1.0 / n))
+        xn, _, _ = tg.oc_update(s_, x0, dc, dv, dv, VOLFRAC, MOVE)
+        first[name] = dict(xf=xf, u=s_.u.copy(), c=c, dc=dc, x_new=xn)
+        s_.close()
 
     # ---- roofline of the dominant kernel (FP32 PCG operator, k_march3) and of the
     #      PCG update, each timed alone with CUDA events on the launching stream
@@ -437,29 +459,39 @@ def run_ours(args):
     full = full_scale_leg(tg, stream, int(os.environ.get("FULL_STEPS", "2")))
 
     cg = [int(s.cg_iterations) for s in stats]
+    roof["fp64_pcg_same_window"] = {"design_iters_per_s": fp64["value"], "fp32ir_vs_fp64": fp64["fp32ir_vs_fp64"]}
     line = {"metric": METRIC, "value": value, "unit": "design_iters/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 K*u and PCG inside f64 refinement",
-            "data": "synthetic",
-            "config": {"workload": WORKLOAD, "method": "FP32-IR + previous-step warm start",
-                       "l2": "working set ~0.3 GB per GPU > 129 MB L2 (no flush)",
-                       "parallelism": "replicas" if ws > 1 else "single GPU"},
+            "data": "synthetic", "config": config_line(),
+            "method": "FP32-IR + previous-step warm start", "parallelism": "replicas" if ws > 1 else "single GPU",
             "clocks": clocks, "e2e": e2e, "gpu_launches": int(launches), "roofline": roof,
-            "fp64_pcg": fp64, "accuracy_vs_fp64": acc, "batched_2d": batched, "learned_warm_start": learned,
+            "fp64_pcg": fp64, "batched_2d": batched, "learned_warm_start": learned,
             "full_scale_256x128x128": full,
             "inner_cg_iters_per_step": cg,
             "outer_iters_per_step": [int(s.outer_iterations) for s in stats],
             "compliance_last": stats[-1].compliance}
     if rank == 0 and not args.no_cpu:
-        os.environ.setdefault("OMP_NUM_THREADS", "1")
-        r = cpu_sample(1, it64, sample_iters=3)
-        line["cpu_baseline"] = {"value": 1.0 / r["seconds_per_design_iter"], "unit": "design_iters/s", "cores": 1,
-                                "kind": "port",
-                                "sample": "oracle port of the reference matrix-free path (per-element Ke, two-phase "
-                                          "gather): filter + compliance + pullback + OC once, 3 Jacobi-PCG iterations "
-                                          "timed and scaled to %d iterations (the FP64 PCG count at the first design "
-                                          "iteration)" % it64,
-                                "seconds_per_pcg_iter": r["seconds_per_pcg_iter"]}
+        threads = cpu_threads()
+        r = cpu_design_iterations(threads, 1, 0.0)
+        sec = r["seconds"][0]
+        line["cpu_baseline"] = {"value": 1.0 / sec, "unit": "design_iters/s", "cores": threads, "kind": "port",
+                                "sample": "design iteration 1, whole: filter, cold Jacobi PCG to rtol 1e-8 (%d "
+                                          "iterations), compliance, pullback, OC" % r["cg_iters"][0]}
+        ref = r["first"]
+
+        def relmax(a, b):
+            return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+
+        acc = {"oracle": "C port of the reference path, FP64 Jacobi PCG to rtol 1e-8, design iteration 1"}
+        for name, g in first.items():
+            acc[name] = {"compliance_rel_err": abs(g["c"] - ref["c"]) / abs(ref["c"]),
+                         "sens_rel_err": relmax(g["dc"], ref["dc"]),
+                         "filtered_density_rel_err": relmax(g["xf"], ref["xf"]),
+                         "displacement_rel_err_2norm": float(np.linalg.norm(g["u"] - ref["u"]) /
+                                                             np.linalg.norm(ref["u"])),
+                         "x_new_max_abs_diff": float(np.max(np.abs(g["x_new"] - ref["x_new"])))}
+        line["accuracy_vs_oracle"] = acc
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:
@@ -561,6 +593,110 @@ def run_rows(args):
     return 0
 
 
+def run_lengths(args):
+    """The configurations at their own run lengths (opt-in, several minutes): the 3D
+    cantilever 160x80x80 for 50 design iterations, the 256 uneven 2D cantilevers for 100,
+    the 3D cantilever 256x128x128 for 200.  FP32-IR with the previous-step start; the
+    compliance trajectory is kept, and at sampled iterations the compliance of the
+    FP32-IR design is recomputed with a cold plain FP64 PCG solve (the FP32-IR error).
+    Plain FP64 PCG runs the first design iterations of each 3D configuration for its
+    rate.  Prints one JSON line per configuration."""
+    import torch
+    import __graft_entry__ as ge
+    tg = ge.load()
+    L = tg._lib
+    stream = torch.cuda.Stream()
+
+    def run3d(nels, volfrac, rmin, iters, samples, fp64_iters):
+        prob = tg.PointLoadCantilever(nels, (1.0, 1.0, 1.0), load="face_centre")
+        n = prob.ncells
+
+        def mk(prec, warm):
+            s = tg.FEASolver(tg.GB300Solver, prob, xmin=XMIN, penalty=tg.PowerPenaltyFun(PEN), rtol=RTOL,
+                             abstol=0.0, cg_max_iter=400000, precision=prec, warm_start=warm)
+            L.check(L.lib().tog_set_stream(s.handle, L.C.c_void_p(stream.cuda_stream)))
+            return s
+        s = mk("fp32_ir", True)
+        loop = tg.SIMPLoop(s, volfrac=volfrac, rmin=rmin, filter="density", x0=np.full(n, volfrac))
+        chk = mk("fp64", False)
+        comp64 = tg.ComplianceFun(chk)
+        traj, cg, errs, t_run = [], [], {}, 0.0
+        for k in range(1, iters + 1):
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            st = loop.step()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            t_run += e0.elapsed_time(e1) / 1e3
+            traj.append(float(st.compliance))
+            cg.append(int(st.cg_iterations))
+            if k in samples:
+                c64 = comp64(tg.PseudoDensities(loop.physical))
+                errs[k] = abs(st.compliance - c64) / abs(c64)
+        s.close()
+        chk.close()
+        s64 = mk("fp64", False)
+        loop64 = tg.SIMPLoop(s64, volfrac=volfrac, rmin=rmin, filter="density", x0=np.full(n, volfrac))
+        torch.cuda.synchronize()
+        g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        g0.record(stream)
+        cg64 = [int(loop64.step(precision="fp64", warm_start=False).cg_iterations) for _ in range(fp64_iters)]
+        g1.record(stream)
+        torch.cuda.synchronize()
+        t64 = g0.elapsed_time(g1) / 1e3
+        s64.close()
+        return {"design_iters": iters, "fp32ir_design_iters_per_s": iters / t_run,
+                "fp32ir_cg_iters_mean": float(np.mean(cg)), "compliance_first_last": [traj[0], traj[-1]],
+                "compliance_every_10": traj[9::10], "fp32ir_vs_fp64_compliance_rel_err": errs,
+                "fp64_pcg": {"design_iters": fp64_iters, "design_iters_per_s": fp64_iters / t64,
+                             "cg_iters": cg64}}
+
+    out = run3d((160, 80, 80), VOLFRAC, RMIN, 50, {1, 10, 25, 50}, 5)
+    print(json.dumps({"config": "3D cantilever 160x80x80, V 0.3, rmin 1.5", **out}), flush=True)
+    P = tg.uneven_cantilever_set(256, seed=0)
+    b = tg.BatchedSIMP(P["nelx"], P["nely"], P["load_j"], P["volfrac"], P["rmin"], rtol=RTOL)
+    rows = b.autotune()
+    b.set_stream(stream.cuda_stream)
+    comps, t_run = [], 0.0
+    for k in range(100):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        st = b.step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t_run += e0.elapsed_time(e1) / 1e3
+        comps.append(b.results()[0].copy())
+    res, nref, status = b.solve_info()
+    b.close()
+    comps = np.array(comps)
+    print(json.dumps({"config": "256 uneven 2D cantilevers (seed 0)", "design_iters": 100, "tile_rows": rows,
+                      "design_iters_per_s": 100 / t_run, "problem_design_iters_per_s": 25600 / t_run,
+                      "compliance_sum_first_last": [float(comps[0].sum()), float(comps[-1].sum())],
+                      "max_final_residual": float(np.max(res)), "failed": int(np.sum(status != 0))}), flush=True)
+    out = run3d((256, 128, 128), 0.2, 2.0, 200, {1, 50, 100, 200}, 2)
+    print(json.dumps({"config": "3D cantilever 256x128x128, V 0.2, rmin 2.0", **out}), flush=True)
+    return 0
+
+
+def run_profile_loop(args):
+    """Launch-list driver of the device SIMP loop: one FP32-IR design iteration of the
+    benchmark workload (160x80x80); prints its PCG iteration and refresh counts so that
+    the kernels ncu lists can be checked against them (no timing; used under ncu)."""
+    import __graft_entry__ as ge
+    tg = ge.load()
+    prob = tg.PointLoadCantilever(NELS, (1.0, 1.0, 1.0), load="face_centre")
+    s = tg.FEASolver(tg.GB300Solver, prob, xmin=XMIN, penalty=tg.PowerPenaltyFun(PEN), rtol=RTOL, abstol=0.0,
+                     cg_max_iter=200000, precision="fp32_ir", warm_start=True)
+    loop = tg.SIMPLoop(s, volfrac=VOLFRAC, rmin=RMIN, filter="density")
+    st = loop.step()
+    print(json.dumps({"design_iterations": 1, "pcg_iterations": int(st.cg_iterations),
+                      "fp64_refreshes": int(st.outer_iterations)}))
+    s.close()
+    return 0
+
+
 def run_profile_batch(args):
     """Profiling driver of the batched 2D operator: the benchmark's 256 uneven cantilevers,
     the band height pinned to args.profile_batch rows, five launches of the FP32 operator
@@ -588,6 +724,9 @@ def main():
     ap.add_argument("--profile", action="store_true", help="run the small ncu driver instead of the benchmark")
     ap.add_argument("--nels", default="256,128,128", help="grid of --profile")
     ap.add_argument("--rows", action="store_true", help="time the entry points beside the headline loop")
+    ap.add_argument("--profile-loop", action="store_true", help="run the device-loop launch-list driver")
+    ap.add_argument("--runs", action="store_true",
+                    help="run the configurations at their own lengths (50 / 100 / 200 design iterations)")
     ap.add_argument("--profile-batch", type=int, default=0, metavar="ROWS",
                     help="run the batched-operator ncu driver with this band height instead of the benchmark")
     args = ap.parse_args()
@@ -597,6 +736,10 @@ def main():
         return run_profile_batch(args)
     if args.rows:
         return run_rows(args)
+    if args.runs:
+        return run_lengths(args)
+    if args.profile_loop:
+        return run_profile_loop(args)
     if args.warmup < 3:
         log("warmup raised to 3 (timing rule)")
         args.warmup = 3

@@ -12,6 +12,9 @@ Sources:
   test/FEA/solvers.jl:32-59                solver-agreement case and tolerance
   test/Functions/test_common_fns.jl:32-49  compliance FD-gradient case and tolerance
   test/CheqFilters/test_filters.jl:71-73    too-small rmin throws
+  test/inp_parser/MBB.inp, parser.jl:36-59  the structured CPS4 MBB mesh (described by its
+                                            lattice, sets, supports, load and material) and
+                                            the parser's asserted values for it
 """
 import json
 import os
@@ -74,7 +77,65 @@ def main(ref):
     )
     with open(os.path.join(HERE, "reference_pins.json"), "w") as f:
         json.dump(pins, f, indent=1)
-    print("wrote metadata_2x2.json and reference_pins.json")
+    inp_mbb(ref)
+    print("wrote metadata_2x2.json, reference_pins.json and inp_mbb.json")
+
+
+def inp_mbb(ref):
+    """MBB.inp is a structured quad mesh: record it as its lattice (checked node by node
+    and cell by cell), its node sets, *BOUNDARY and *CLOAD entries and material, and the
+    values test/inp_parser/parser.jl asserts for it."""
+    text = open(os.path.join(ref, "test/inp_parser/MBB.inp")).read().splitlines()
+    sec, nodes, cells, nsets, bcs, cl, mat = None, [], [], {}, [], [], None
+    for i, line in enumerate(text):
+        if line.startswith("*"):
+            sec = line
+            if line.startswith("*NSET"):
+                nsets[re.search(r"NSET\s*=\s*([^,\s]*)", line).group(1)] = []
+            if line.startswith("*ELASTIC"):
+                mat = [float(v) for v in text[i + 1].split(",")]
+            continue
+        v = [t.strip() for t in line.split(",") if t.strip()]
+        if not v:
+            continue
+        if sec.startswith("*Node"):
+            nodes.append([float(t) for t in v[1:]])
+        elif sec.startswith("*Element"):
+            cells.append([int(t) for t in v[1:]])
+        elif sec.startswith("*NSET"):
+            list(nsets.values())[-1].extend(int(t) for t in v)
+        elif sec.startswith("*BOUNDARY"):
+            bcs.append([v[0], int(v[1])])
+        elif sec.startswith("*CLOAD"):
+            cl.append([int(v[0]), int(v[1]), float(v[2])])
+    xs = sorted({c[0] for c in nodes})
+    ys = sorted({c[1] for c in nodes})
+    nnx, h = len(xs), xs[1] - xs[0]
+    for k, c in enumerate(nodes):   # x fastest from id 1, spacing h, origin (0, 0)
+        assert c == [h * (k % nnx), h * (k // nnx)], k
+    for e, c in enumerate(cells):   # x fastest, corners (n, n+1, n+1+nnx, n+nnx)
+        n = 1 + e % (nnx - 1) + nnx * (e // (nnx - 1))
+        assert c == [n, n + 1, n + 1 + nnx, n + nnx], e
+    par = open(os.path.join(ref, "test/inp_parser/parser.jl")).read()
+    blk = par.split('extract_inp(joinpath(@__DIR__, "MBB.inp"))')[1].split("extract_inp")[0]
+    pins = dict(
+        celltype=re.search(r'celltype == "(\w+)"', blk).group(1),
+        node_coords={k: [float(a), float(b)] for k, a, b in
+                     re.findall(r"node_coords\[(\d+)\] == \(([-\d.]+), ([-\d.]+)\)", blk)},
+        cells={k: [int(t) for t in v.split(",")] for k, v in re.findall(r"cells\[(\d+)\] == \(([\d, ]+)\)", blk)},
+        nodedbcs={k: [[int(a), float(b)] for a, b in re.findall(r"\((\d+), ([-\d.]+)\)", v)]
+                  for k, v in re.findall(r'nodedbcs\["(\w+)"\] == \[(.*?)\]\n', blk)},
+        cloads={k: [float(t) for t in v.split(",")] for k, v in re.findall(r"cloads\[(\d+)\] == \[([-\d., ]+)\]", blk)},
+        density=float(re.search(r"density == ([-\d.]+)", blk).group(1)),
+        E=float(re.search(r"\.E == ([-\d.]+)", blk).group(1)),
+        nu=float(re.search(r"\.ν == ([-\d.]+)", blk).group(1)))
+    out = dict(source="test/inp_parser/MBB.inp; asserted values test/inp_parser/parser.jl:36-59",
+               lattice=dict(nn=[nnx, len(ys)], spacing=[h, ys[1] - ys[0]], origin=[0.0, 0.0],
+                            celltype="CPS4", node_order="x fastest from 1",
+                            cell_order="x fastest, corners (n, n+1, n+1+nnx, n+nnx)"),
+               nsets=nsets, boundary=bcs, cload=cl, material=mat, pins=pins)
+    with open(os.path.join(HERE, "inp_mbb.json"), "w") as f:
+        json.dump(out, f, indent=1)
 
 
 if __name__ == "__main__":

@@ -13,7 +13,10 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def test_learned_warm_start_gain(tg):
+def test_learned_warm_start_trains_and_keeps_the_trajectory(tg):
+    """What is asserted: the network trains (loss halves), and every start reaches the
+    same designs.  The learned start's PCG iterations relative to the previous-step start
+    are reported, not asserted: measured, the learned start does not gain (ratio >= 1)."""
     from topopt_gb300 import learned as LW
     nels = (32, 16, 16)
     runs = LW.sample_runs(3, nels, seed=5)
@@ -28,6 +31,6 @@ def test_learned_warm_start_gain(tg):
         assert abs(c[m] - c["previous"]) <= 1e-6 * abs(c["previous"]), (m, c)
     its = {m: r["cg_iters_mean"] for m, r in ev.items()}
     print("mean PCG iterations per design iteration:", its,
-          "learned / previous = %.3f" % (its["learned"] / its["previous"]))
+          "learned / previous = %.3f (below 1 would be a gain)" % (its["learned"] / its["previous"]))
     assert all(np.isfinite(v) and v > 0 for v in its.values())
     net.close()

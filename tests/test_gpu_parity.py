@@ -104,8 +104,12 @@ def test_compliance_and_sensitivities(tg, O, nels, kind, pen):
 
 @pytest.mark.parametrize("nels,kind,rmin", [((5, 5), "mbb", 2.0), ((12, 6), "mbb", 1.5), ((60, 20), "mbb", 2.0),
                                             ((16, 8), "cant", 3.0), ((6, 4, 4), "cant", 1.5),
-                                            ((6, 4, 4), "cant", 2.0), ((8, 4, 6), "mbb", 2.5)])
+                                            ((6, 4, 4), "cant", 2.0), ((8, 4, 6), "mbb", 2.5),
+                                            ((70, 20, 34), "cant", 1.5), ((40, 18, 20), "cant", 3.0),
+                                            ((12, 8, 8), "cant", 8.0), ((100, 30), "mbb", 9.0)])
 def test_filters_match_oracle(tg, O, nels, kind, rmin):
+    """The shared-memory stencil kernels (z bands, tiles ending inside the grid) and, for
+    the 3D rmin = 8 stencil that does not fit in shared memory, the two-pass kernels."""
     p, op = make(tg, O, nels, kind)
     s = tg.FEASolver(tg.GB300Solver, p)
     df = tg.DensityFilterFun(s, rmin)

@@ -8,6 +8,7 @@ __graft_entry__.py; the directory name carries a dot).
 """
 from ._lib import TopOptError, NotConverged, lib  # noqa: F401
 from .vtk import save_mesh  # noqa: F401
+from .inp import InpContent, InpStiffness, parse_inp, write_inp  # noqa: F401
 from .topopt_api import (  # noqa: F401
     BatchedSIMP,
     BlockComplianceFun,

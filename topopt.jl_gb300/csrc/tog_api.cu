@@ -17,6 +17,7 @@
 #include "tog_kernels.cuh"
 #include "tog_mv3.cuh"
 #include "tog_march3.cuh"
+#include "tog_filter.cuh"
 #include "tog_mma.cuh"
 
 using namespace tog;
@@ -48,7 +49,6 @@ int fail(int code, const std::string& msg) {
 #define TOG_LAUNCHED(n) g_launches.fetch_add((n), std::memory_order_relaxed)
 
 constexpr int kEwThreads = 256;
-constexpr int kPcgBatch = 32;   // PCG iterations per graph launch
 constexpr int kOcMaxSteps = 100;
 
 }  // namespace
@@ -108,6 +108,10 @@ struct tog_handle {
     double* d_invW = nullptr;
     bool filter_ready = false;
     double rmin = 0;
+    FiltBox fbox{};            // node-offset range of the stencil
+    bool filt_fused = false;   // shared-memory stencil kernels (else the two-pass kernels)
+    int filt_lz = 1;           // cell planes per z band of the fused kernels
+    size_t filt_smem[2] = {0, 0};
     // state
     bool vars_dirty = true;
     bool u_valid = false;
@@ -355,7 +359,7 @@ void launch_matvec(tog_handle* h, cudaStream_t s, const T* x, T* y, const double
 }
 
 template <typename T>
-void launch_pcg_update(tog_handle* h, cudaStream_t s) {
+void launch_pcg_update(tog_handle* h, cudaStream_t s, LoopCond cond = LoopCond{}) {
     const int nb = h->ew_blocks(h->nnodes);
     if (h->dim == 3) {
         Mv3Args<T> A = mv3_args<T>(h);
@@ -371,15 +375,15 @@ void launch_pcg_update(tog_handle* h, cudaStream_t s) {
             k_side_gather3<T><<<(int)nbs, kEwThreads, 0, s>>>(A);
             TOG_LAUNCHED(1);
         }
-        k_pcg_update3<T><<<h->upd_blocks(), kEwThreads, 0, s>>>(A, x, r, (T)h->meandiag);
+        k_pcg_update3<T><<<h->upd_blocks(), kEwThreads, 0, s>>>(A, x, r, (T)h->meandiag, cond);
     } else if (std::is_same<T, double>::value) {
             k_pcg_update<double, 2><<<nb, kEwThreads, 0, s>>>(h->d_u, h->d_r64, h->d_p64[0], h->d_p64[1], h->d_q64,
                                                               h->d_dinv64, h->M2d, h->nnodes, h->d_st64,
-                                                              h->d_partials);
+                                                              h->d_partials, cond);
     } else {
             k_pcg_update<float, 2><<<nb, kEwThreads, 0, s>>>(h->d_x32, h->d_r32, h->d_p32[0], h->d_p32[1], h->d_q32,
                                                              h->d_dinv32, h->M2f, h->nnodes, h->d_st32,
-                                                             h->d_partials);
+                                                             h->d_partials, cond);
     }
     TOG_LAUNCHED(1);
 }
@@ -410,28 +414,57 @@ void launch_pcg_init(tog_handle* h, cudaStream_t s, int zero_x, double rtol, dou
     TOG_LAUNCHED(1);
 }
 
-// Graph of kPcgBatch PCG iterations (operator + update per iteration).  Kernels
-// read the iteration state from device memory and return at once after
-// convergence, so one graph serves every batch of every solve.
+// The PCG iterations of one solve segment as ONE graph launch: a conditional WHILE
+// node whose body is the operator, the update (and the EnergyCriteria check).  A
+// first kernel sets the condition from the state (nothing runs if it is already
+// done); the update's last block clears it once the state is done (converged,
+// maxiter, breakdown or a reliable-update pause), so the loop stops on the device
+// with no operator or update launched after convergence.
+__global__ void k_pcg_cond_init(const PcgState* __restrict__ st, cudaGraphConditionalHandle h) {
+    if (threadIdx.x == 0) cudaGraphSetConditional(h, st->done ? 0u : 1u);
+}
+
 template <typename T>
 int build_pcg_graph(tog_handle* h, cudaGraphExec_t* out, bool energy = false) {
+    PcgState* d_st = std::is_same<T, double>::value ? h->d_st64 : h->d_st32;
     cudaGraph_t g = nullptr;
-    TOG_CUDA(cudaStreamBeginCapture(h->own, cudaStreamCaptureModeThreadLocal));
-    const long long before = g_launches.load();
-    for (int i = 0; i < kPcgBatch; ++i) {
-        launch_matvec<T, MV_PCG>(h, h->own, nullptr, nullptr, nullptr);
-        launch_pcg_update<T>(h, h->own);
-        if (energy) {
-            k_energy_check<<<h->ew_blocks(h->ndofs), kEwThreads, 0, h->own>>>(h->d_u, h->d_r64, h->d_f, h->ndofs,
-                                                                             h->d_st64, h->d_partials);
-            TOG_LAUNCHED(1);
-        }
+    TOG_CUDA(cudaGraphCreate(&g, 0));
+    cudaGraphConditionalHandle ch;
+    TOG_CUDA(cudaGraphConditionalHandleCreate(&ch, g, 0, cudaGraphCondAssignDefault));
+    // the condition from the state
+    cudaGraphNode_t init;
+    {
+        cudaKernelNodeParams kp{};
+        void* args[2] = {(void*)&d_st, (void*)&ch};
+        kp.func = (void*)k_pcg_cond_init;
+        kp.gridDim = dim3(1);
+        kp.blockDim = dim3(32);
+        kp.kernelParams = args;
+        TOG_CUDA(cudaGraphAddKernelNode(&init, g, nullptr, 0, &kp));
     }
-    // kernels per batch; captured launches run only when the graph is launched
+    cudaGraphNodeParams cp{};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = ch;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t loop;
+    TOG_CUDA(cudaGraphAddNode(&loop, g, &init, nullptr, 1, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    TOG_CUDA(cudaStreamBeginCaptureToGraph(h->own, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    const long long before = g_launches.load();
+    launch_matvec<T, MV_PCG>(h, h->own, nullptr, nullptr, nullptr);
+    launch_pcg_update<T>(h, h->own, LoopCond{ch, 1});
+    if (energy) {
+        k_energy_check<<<h->ew_blocks(h->ndofs), kEwThreads, 0, h->own>>>(h->d_u, h->d_r64, h->d_f, h->ndofs,
+                                                                         h->d_st64, h->d_partials);
+        TOG_LAUNCHED(1);
+    }
+    // kernels per iteration; captured launches run only when the graph is launched
     const int nodes = (int)(g_launches.load() - before);
     g_launches.fetch_sub(nodes);
     (std::is_same<T, double>::value ? h->graph_nodes64 : h->graph_nodes32) = nodes;
-    TOG_CUDA(cudaStreamEndCapture(h->own, &g));
+    cudaGraph_t cap = nullptr;
+    TOG_CUDA(cudaStreamEndCapture(h->own, &cap));
     TOG_CUDA(cudaGraphInstantiate(out, g, 0));
     cudaGraphDestroy(g);
     return TOG_OK;
@@ -443,18 +476,22 @@ int sync_state(tog_handle* h, const PcgState* d_st) {
     return TOG_OK;
 }
 
-// Run graph batches until the PCG state says done.
+// Run the PCG iterations of the current state to done: one graph launch, one host
+// synchronisation.
 template <typename T>
 int run_pcg(tog_handle* h, bool energy = false) {
     cudaGraphExec_t* g = std::is_same<T, double>::value ? (energy ? &h->g_pcg64e : &h->g_pcg64) : &h->g_pcg32;
     PcgState* d_st = std::is_same<T, double>::value ? h->d_st64 : h->d_st32;
     if (!*g) TOG_TRY(build_pcg_graph<T>(h, g, energy));
     TOG_TRY(sync_state(h, d_st));
-    while (!h->h_st->done) {
-        TOG_CUDA(cudaGraphLaunch(*g, h->stream));
-        TOG_LAUNCHED((std::is_same<T, double>::value ? h->graph_nodes64 : h->graph_nodes32));
-        TOG_TRY(sync_state(h, d_st));
-    }
+    const int it0 = h->h_st->it;
+    if (h->h_st->done) return TOG_OK;
+    TOG_CUDA(cudaGraphLaunch(*g, h->stream));
+    TOG_TRY(sync_state(h, d_st));
+    // launches of this segment: the condition kernel and the body of every iteration run
+    // (plus at most one body that found the state done)
+    TOG_LAUNCHED(1 + (long long)(h->h_st->it - it0 + 1) *
+                         (std::is_same<T, double>::value ? h->graph_nodes64 : h->graph_nodes32));
     return TOG_OK;
 }
 
@@ -843,6 +880,29 @@ int filter_dev(tog_handle* h, int op, const double* in, double* out) {
     const Dims D = h->dims();
     const int nbn = h->ew_blocks(h->nnodes), nbc = h->ew_blocks(h->ncells);
     cudaStream_t s = h->stream;
+    if (h->filt_fused) {
+        const dim3 grid((D.nel[0] + kFiltTX - 1) / kFiltTX, (D.nel[1] + kFiltTY - 1) / kFiltTY,
+                        h->dim == 3 ? (D.nel[2] + h->filt_lz - 1) / h->filt_lz : 1);
+        const int nt = kFiltTX * kFiltTY;
+        if (op == TOG_FILTER_J) {
+            if (h->dim == 3)
+                k_filt_fwd<3><<<grid, nt, h->filt_smem[0], s>>>(in, out, h->d_soff, h->d_sw, h->S, h->d_invW, D,
+                                                                h->fbox, h->filt_lz);
+            else
+                k_filt_fwd<2><<<grid, nt, h->filt_smem[0], s>>>(in, out, h->d_soff, h->d_sw, h->S, h->d_invW, D,
+                                                                h->fbox, 1);
+        } else {
+            if (h->dim == 3)
+                k_filt_bwd<3><<<grid, nt, h->filt_smem[1], s>>>(in, out, h->d_soff, h->d_sw, h->S, h->d_invW, D,
+                                                                h->fbox, h->filt_lz);
+            else
+                k_filt_bwd<2><<<grid, nt, h->filt_smem[1], s>>>(in, out, h->d_soff, h->d_sw, h->S, h->d_invW, D,
+                                                                h->fbox, 1);
+        }
+        TOG_LAUNCHED(1);
+        TOG_CUDA(cudaGetLastError());
+        return TOG_OK;
+    }
     if (op == TOG_FILTER_J) {
         if (h->dim == 3) {
             k_filt_node_avg<3><<<nbn, kEwThreads, 0, s>>>(in, h->d_nodal, D);
@@ -865,16 +925,44 @@ int filter_dev(tog_handle* h, int op, const double* in, double* out) {
     return TOG_OK;
 }
 
+// The OC bisection as one graph: a conditional WHILE node over k_oc_step (whose last
+// block stops the loop once the bisection has converged or run kOcMaxSteps steps), then
+// the new design.
 int build_oc_graph(tog_handle* h) {
     cudaGraph_t g = nullptr;
-    TOG_CUDA(cudaStreamBeginCapture(h->own, cudaStreamCaptureModeThreadLocal));
+    TOG_CUDA(cudaGraphCreate(&g, 0));
+    cudaGraphConditionalHandle ch;
+    TOG_CUDA(cudaGraphConditionalHandleCreate(&ch, g, 0, cudaGraphCondAssignDefault));
+    OcState* d_oc = h->d_oc;
+    cudaGraphNode_t init;
+    {
+        cudaKernelNodeParams kp{};
+        void* args[2] = {(void*)&d_oc, (void*)&ch};
+        kp.func = (void*)k_oc_cond_init;
+        kp.gridDim = dim3(1);
+        kp.blockDim = dim3(32);
+        kp.kernelParams = args;
+        TOG_CUDA(cudaGraphAddKernelNode(&init, g, nullptr, 0, &kp));
+    }
+    cudaGraphNodeParams cp{};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = ch;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t loop;
+    TOG_CUDA(cudaGraphAddNode(&loop, g, &init, nullptr, 1, &cp));
     const int nb = h->ew_blocks(h->ncells);
-    for (int i = 0; i < kOcMaxSteps; ++i)
-        k_oc_step<<<nb, kEwThreads, 0, h->own>>>(h->d_x, h->d_B, h->d_w, h->ncells, h->d_oc, h->d_partials,
-                                                 h->d_fpos);
+    TOG_CUDA(cudaStreamBeginCaptureToGraph(h->own, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                           cudaStreamCaptureModeThreadLocal));
+    k_oc_step<<<nb, kEwThreads, 0, h->own>>>(h->d_x, h->d_B, h->d_w, h->ncells, h->d_oc, h->d_partials, h->d_fpos,
+                                             LoopCond{ch, 1});
+    cudaGraph_t body = nullptr;
+    TOG_CUDA(cudaStreamEndCapture(h->own, &body));
+    TOG_CUDA(cudaStreamBeginCaptureToGraph(h->own, g, &loop, nullptr, 1, cudaStreamCaptureModeThreadLocal));
     k_oc_final<<<nb, kEwThreads, 0, h->own>>>(h->d_x, h->d_B, h->d_xnew, h->ncells, h->d_oc, h->d_partials,
                                                h->d_w, h->d_fpos);
-    TOG_CUDA(cudaStreamEndCapture(h->own, &g));
+    cudaGraph_t cap = nullptr;
+    TOG_CUDA(cudaStreamEndCapture(h->own, &cap));
     TOG_CUDA(cudaGraphInstantiate(&h->g_oc, g, 0));
     cudaGraphDestroy(g);
     return TOG_OK;
@@ -889,9 +977,9 @@ int oc_dev(tog_handle* h, double volfrac, double move) {
     TOG_LAUNCHED(1);
     TOG_CUDA(cudaGetLastError());
     TOG_CUDA(cudaGraphLaunch(h->g_oc, h->stream));
-    TOG_LAUNCHED(kOcMaxSteps + 1);
     TOG_CUDA(cudaMemcpyAsync(h->h_oc, h->d_oc, sizeof(OcState), cudaMemcpyDeviceToHost, h->stream));
     TOG_CUDA(cudaStreamSynchronize(h->stream));
+    TOG_LAUNCHED(2 + h->h_oc->steps);   // condition, every bisection step, final
     return TOG_OK;
 }
 
@@ -1609,6 +1697,42 @@ int tog_filter_setup(tog_handle* h, double rmin) {
     TOG_CUDA(cudaMemcpyAsync(h->d_soff, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice, h->stream));
     TOG_CUDA(cudaMemcpyAsync(h->d_sw, w.data(), w.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
     h->S = S;
+    {   // the stencil's node-offset box decides between the fused and the two-pass kernels
+        FiltBox B{};
+        for (int d = 0; d < 3; ++d) {
+            B.lo[d] = 1 << 30;
+            B.hi[d] = -(1 << 30);
+        }
+        for (int k = 0; k < S; ++k)
+            for (int d = 0; d < 3; ++d) {
+                B.lo[d] = std::min(B.lo[d], off[3 * k + d]);
+                B.hi[d] = std::max(B.hi[d], off[3 * k + d]);
+            }
+        h->fbox = B;
+        h->filt_smem[0] = filt_fwd_smem(B, S, h->dim);
+        h->filt_smem[1] = filt_bwd_smem(B, S, h->dim);
+        h->filt_fused = std::max(h->filt_smem[0], h->filt_smem[1]) <= kFiltMaxSmem;
+        if (h->filt_fused) {
+            if (h->dim == 3) {
+                TOG_CUDA(cudaFuncSetAttribute(k_filt_fwd<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)h->filt_smem[0]));
+                TOG_CUDA(cudaFuncSetAttribute(k_filt_bwd<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)h->filt_smem[1]));
+                // z bands: about two blocks per SM, at least 8 cell planes each
+                const long long tiles = (long long)((h->nel[0] + kFiltTX - 1) / kFiltTX) *
+                                        ((h->nel[1] + kFiltTY - 1) / kFiltTY);
+                long long nb = std::max(1LL, (2LL * h->nsm + tiles - 1) / tiles);
+                nb = std::min<long long>(nb, std::max(1, h->nel[2] / 8));
+                h->filt_lz = (int)((h->nel[2] + nb - 1) / nb);
+            } else {
+                TOG_CUDA(cudaFuncSetAttribute(k_filt_fwd<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)h->filt_smem[0]));
+                TOG_CUDA(cudaFuncSetAttribute(k_filt_bwd<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)h->filt_smem[1]));
+                h->filt_lz = 1;
+            }
+        }
+    }
     if (h->dim == 3)
         k_filt_invW<3><<<h->ew_blocks(h->ncells), kEwThreads, 0, h->stream>>>(h->d_soff, h->d_sw, S, h->d_invW,
                                                                               h->dims());

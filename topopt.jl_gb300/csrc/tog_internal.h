@@ -33,6 +33,19 @@ struct Modal {
     T kdinv[DIM];   // 1 / Ke(a,a) for component c (identical at every corner)
 };
 
+// Condition of a conditional WHILE graph node that runs a loop on the device (the PCG
+// iterations, the OC bisection): the loop's last kernel sets it to "continue" while the
+// state is not done.  `on` is 0 for launches outside such a graph.
+struct LoopCond {
+    cudaGraphConditionalHandle h;
+    int on;
+};
+#ifdef __CUDACC__
+__device__ __forceinline__ void loop_cond_set(const LoopCond& c, bool go) {
+    if (c.on) cudaGraphSetConditional(c.h, go ? 1u : 0u);
+}
+#endif
+
 // Modes of the matrix-free operator kernels: y = K x, the fused PCG direction
 // update + K p + p.q, and the FP64 residual f - K x.
 enum { MV_PLAIN = 0, MV_PCG = 1, MV_RESID = 2 };

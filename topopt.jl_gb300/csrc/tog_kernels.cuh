@@ -342,8 +342,12 @@ template <typename T, int DIM>
 __global__ void __launch_bounds__(256) k_pcg_update(T* __restrict__ x, T* __restrict__ r, const T* __restrict__ P0,
                                                     const T* __restrict__ P1, const T* __restrict__ q,
                                                     const T* __restrict__ dinv, const Modal<T, DIM> M,
-                                                    long long nnodes, PcgState* st, double* partials) {
-    if (st->done) return;
+                                                    long long nnodes, PcgState* st, double* partials,
+                                                    const LoopCond cond) {
+    if (st->done) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) loop_cond_set(cond, false);
+        return;
+    }
     const int it = st->it;
     const T* __restrict__ p = (it & 1) ? P1 : P0;
     const T alpha = (T)st->alpha;
@@ -384,6 +388,7 @@ __global__ void __launch_bounds__(256) k_pcg_update(T* __restrict__ x, T* __rest
                 st->done = 1;
             }
             st->rr_max = fmax(st->rr_max, tot[1]);
+            loop_cond_set(cond, !st->done);
         }
     }
 }
@@ -782,8 +787,12 @@ __global__ void __launch_bounds__(256) k_oc_prep(const double* __restrict__ x, c
 
 __global__ void __launch_bounds__(256) k_oc_step(const double* __restrict__ x, const double* __restrict__ B,
                                                  const double* __restrict__ w, long long n, OcState* oc,
-                                                 double* partials, const int* __restrict__ fpos) {
-    if (oc->done) return;
+                                                 double* partials, const int* __restrict__ fpos,
+                                                 const LoopCond cond) {
+    if (oc->done) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) loop_cond_set(cond, false);
+        return;
+    }
     const double lmid = 0.5 * (oc->l2 + oc->l1);
     const double s = 1.0 / sqrt(lmid);
     const double move = oc->move;
@@ -803,8 +812,14 @@ __global__ void __launch_bounds__(256) k_oc_step(const double* __restrict__ x, c
                 oc->l2 = lmid;
             oc->steps += 1;
             if ((oc->l2 - oc->l1) / (oc->l1 + oc->l2) <= oc->tol || oc->steps >= oc->maxsteps) oc->done = 1;
+            loop_cond_set(cond, !oc->done);
         }
     }
+}
+
+// Sets a WHILE node's condition from an OC state (the bisection runs unless it is done).
+__global__ void k_oc_cond_init(const OcState* __restrict__ oc, cudaGraphConditionalHandle h) {
+    if (threadIdx.x == 0) cudaGraphSetConditional(h, oc->done ? 0u : 1u);
 }
 
 __global__ void __launch_bounds__(256) k_oc_final(const double* __restrict__ x, const double* __restrict__ B,

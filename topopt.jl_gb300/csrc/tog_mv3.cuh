@@ -537,9 +537,12 @@ __global__ void __launch_bounds__(256) k_mv3_finalize(const Mv3Args<T> A, const 
 // dof arrays are streamed as float4 (4 dofs per thread and step).
 template <typename T>
 __global__ void __launch_bounds__(256) k_pcg_update3(const Mv3Args<T> A, T* __restrict__ x, T* __restrict__ r,
-                                                     T meandiag) {
+                                                     T meandiag, const LoopCond cond) {
     PcgState* st = A.st;
-    if (st->done) return;
+    if (st->done) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) loop_cond_set(cond, false);
+        return;
+    }
     const int it = st->it;
     const T* __restrict__ p = (it & 1) ? A.P1 : A.P0;
     const T* __restrict__ q = A.q;
@@ -651,6 +654,7 @@ __global__ void __launch_bounds__(256) k_pcg_update3(const Mv3Args<T> A, T* __re
                 st->done = 1;
             }
             st->rr_max = fmax(st->rr_max, tot[1]);
+            loop_cond_set(cond, !st->done);
         }
     }
 }
