@@ -275,6 +275,8 @@ def learned_leg(tg, steps):
     out["learned_vs_cold_cg"] = ev["learned"]["cg_iters_mean"] / ev["cold"]["cg_iters_mean"]
     out["compliance_spread_last"] = float(np.ptp([r["compliance"][-1] for r in ev.values()]) /
                                           abs(prev["compliance"][-1]))
+    # the most any predicted start could save on this run (exact solution blended in)
+    out["start_quality_bound"] = LW.start_quality_bound(nels, run, k=8)
     return out
 
 

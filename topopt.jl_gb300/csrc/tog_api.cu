@@ -1974,6 +1974,7 @@ int tog_simp_step(tog_handle* h, int32_t precision, double rtol, int32_t maxiter
     tog_solve_stats ss{};
     int rc = do_solve(h, precision, rtol, 0.0, maxiter, warm_start != 0, &ss);
     if (rc != TOG_OK && rc != TOG_NOT_CONVERGED) return rc;
+    if (learned) TOG_TRY(nn_status(h->net, h->stream));
     if (record) {
         k_nn_target<<<h->ew_blocks(h->ndofs), kEwThreads, 0, h->stream>>>(h->d_u, h->d_uprev, h->d_nn_sc, h->rec_tgt,
                                                                          h->ndofs);

@@ -12,7 +12,9 @@
 // plane of invW d, accumulates one node plane of M2' (valence(n) sum_s w_s
 // (invW d)_{n - off_s}) from a shared ring of those planes, and forms one output
 // cell plane from the two latest node planes (M1': sum over the corners of
-// nodal_n / valence(n)).  The nodal intermediate never leaves the SM.
+// nodal_n / valence(n)).  The nodal intermediate never leaves the SM.  Both kernels
+// are bound by the FP64 pipe (GB300 runs FP64 at a small fraction of its FP32 rate),
+// so they skip the valence factors, which cancel exactly (below).
 #pragma once
 #include <cuda_runtime.h>
 
@@ -43,9 +45,11 @@ inline size_t filt_bwd_smem(const FiltBox& B, int S, int dim) {
            sizeof(int) * 3 * S;
 }
 
-// 1 / k for the cell counts and valences of a structured grid (1, 2, 4 or 8): exact, so
-// the product equals the quotient bit for bit.
-__device__ __forceinline__ double inv_pow2(int k) { return k == 8 ? 0.125 : k == 4 ? 0.25 : k == 2 ? 0.5 : 1.0; }
+// The valence of a node of a structured grid (the number of cells around it) is a power
+// of two and equals the number of cells its average is taken over, so the reference's
+// w_s * valence(n) * (sum / valence(n)) equals w_s * sum bit for bit (scaling by a power
+// of two is exact); the transpose's valence(n) * acc / valence(n) likewise equals acc.
+// The kernels therefore carry nodal sums, not means, and apply no valence at all.
 
 __device__ __forceinline__ int pmod(int a, int m) {
     const int r = a % m;
@@ -97,7 +101,6 @@ __global__ void __launch_bounds__(kFiltTX * kFiltTY) k_filt_fwd(const double* __
           for (int ax = tx; ax < nxn; ax += kFiltTX) {
             const int ix = nx0 + ax, iy = ny0 + ay;
             double s = 0.0;
-            int cnt = 0;
 #pragma unroll
             for (int bz = 0; bz < (DIM == 3 ? 2 : 1); ++bz) {
                 const int cz = iz - 1 + bz;
@@ -108,13 +111,10 @@ __global__ void __launch_bounds__(kFiltTX * kFiltTY) k_filt_fwd(const double* __
 #pragma unroll
                     for (int bx = 0; bx < 2; ++bx) {
                         const int cx = ix - 1 + bx, cy = iy - 1 + by;
-                        if (cx >= 0 && cx < D.nel[0] && cy >= 0 && cy < D.nel[1]) {
-                            s += c[(ay + by) * nxc + (ax + bx)];
-                            ++cnt;
-                        }
+                        if (cx >= 0 && cx < D.nel[0] && cy >= 0 && cy < D.nel[1]) s += c[(ay + by) * nxc + (ax + bx)];
                     }
             }
-            dst[ay * nxn + ax] = s * inv_pow2(cnt);
+            dst[ay * nxn + ax] = s;
           }
     };
     auto out_plane = [&](int ez) {
@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(kFiltTX * kFiltTY) k_filt_fwd(const double* __
                     (DIM == 3 && (iz < 0 || iz >= D.nn[2])))
                     continue;
                 const double* np = nodal + (DIM == 3 ? pmod(iz, nzr) : 0) * nxn * nyn;
-                acc += w[s] * valence<DIM>(ix, iy, iz, D) * np[(iy - ny0) * nxn + (ix - nx0)];
+                acc += w[s] * np[(iy - ny0) * nxn + (ix - nx0)];
             }
             const double iw = invW[e];
             y[e] = iw > 0.0 ? acc * iw : x[e];
@@ -214,7 +214,7 @@ __global__ void __launch_bounds__(kFiltTX * kFiltTY) k_filt_bwd(const double* __
                 const double* p = wd + (DIM == 3 ? pmod(cz, nzr) : 0) * nxc * nyc;
                 acc += w[s] * p[(cy - cy0) * nxc + (cx - cx0)];
             }
-            dst[i] = acc * valence<DIM>(ix, iy, iz, D);
+            dst[i] = acc;
           }
     };
     // output cell plane ez from node planes ez (lo) and ez + 1 (hi)
@@ -228,7 +228,7 @@ __global__ void __launch_bounds__(kFiltTX * kFiltTY) k_filt_bwd(const double* __
             for (int j = 0; j < (1 << DIM); ++j) {
                 const int bx = j & 1, by = (j >> 1) & 1, bz = (j >> 2) & 1;
                 const double* np = bz ? nhi : nlo;
-                s += np[(ay + by) * nxn + (ax + bx)] * inv_pow2(valence<DIM>(ex + bx, ey + by, ez + bz, D));
+                s += np[(ay + by) * nxn + (ax + bx)];
             }
             y[ex + (long long)D.nel[0] * ey + cplane * ez] = s;
         }

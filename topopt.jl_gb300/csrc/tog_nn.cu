@@ -16,12 +16,14 @@
 //   out: 16 -> 16 (3 used), no activation, FP32
 // Input channels 0..7 (8..15 zero), output channels 0..2.
 //
-// Convolutions are implicit GEMMs on the tensor cores (mma.sync m16n8k16, BF16
-// operands, FP32 accumulation): rows = output voxels, columns = output channels,
-// reduction = 27 taps x input channels.  The same kernel computes the
-// transposed convolution of the backward pass (input gradients); weight
-// gradients are a split-K GEMM over voxels.  Training keeps FP32 master weights
-// (Adam); the BF16 copies (and their transposes) are refreshed after each step.
+// Convolutions are implicit GEMMs on the tcgen05 tensor cores (kind::f16, BF16
+// operands staged in shared memory, FP32 accumulators in TMEM; tog_tc.cuh): rows =
+// output voxels, columns = output channels, reduction = 27 taps x input channels.
+// The same kernel computes the transposed convolution of the backward pass (input
+// gradients); weight gradients are a GEMM with rows = (tap, input channel), columns =
+// output channels and the reduction over voxels, split over blocks.  Training keeps
+// FP32 master weights (Adam); the BF16 copies (and their transposes) are refreshed
+// after each step.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -35,6 +37,7 @@
 #include "../../include/topopt_gb300.h"
 #include "tog_internal.h"
 #include "tog_nn.h"
+#include "tog_tc.cuh"
 
 using namespace tog;
 
@@ -73,24 +76,6 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
     return *reinterpret_cast<uint32_t*>(&v);
 }
 
-__device__ __forceinline__ uint32_t load_pair(const bf16* p, long long off, bool ok) {
-    return ok ? *reinterpret_cast<const uint32_t*>(p + off) : 0u;
-}
-__device__ __forceinline__ uint32_t load_pair(const float* p, long long off, bool ok) {
-    if (!ok) return 0u;
-    const float2 v = *reinterpret_cast<const float2*>(p + off);
-    return pack_bf16(v.x, v.y);
-}
-
-__device__ __forceinline__ void mma_bf16(float (&c)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
-                                         uint32_t b0, uint32_t b1) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};\n"
-        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
-}
-
 // voxel index -> (n, z, y, x)
 __device__ __forceinline__ void vox_coords(const Vol& v, long long m, int& n, int& z, int& y, int& x) {
     x = (int)(m % v.w);
@@ -125,155 +110,277 @@ __device__ __forceinline__ bool src_voxel(const ConvArgs& a, int n, int z, int y
     return true;
 }
 
-// Implicit-GEMM 3x3x3 convolution.  A warp computes 16 destination voxels x
-// 8*NT destination channels (NT = cdst / 8), a block 4 warps.
-template <typename TA, typename TO, int NT, bool TRANSPOSED>
-__global__ void __launch_bounds__(128) k_conv(ConvArgs a) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int g = lane >> 2, t = lane & 3;
-    const long long M = a.dst.vox();
-    const long long m0 = ((long long)blockIdx.x * 4 + warp) * 16;
-    if (m0 >= M) return;
-    int rn[2], rz[2], ry[2], rx[2];
-    bool rv[2];
-#pragma unroll
-    for (int r = 0; r < 2; ++r) {
-        const long long m = m0 + g + 8 * r;
-        rv[r] = m < M;
-        vox_coords(a.dst, rv[r] ? m : 0, rn[r], rz[r], ry[r], rx[r]);
-    }
-    float acc[NT][4];
-#pragma unroll
-    for (int j = 0; j < NT; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
-    const TA* A = reinterpret_cast<const TA*>(a.A);
-    const int kchunks = a.csrc >> 4;
-    const long long wstride = 27LL * a.csrc;   // one destination channel's weights
-    for (int tap = 0; tap < 27; ++tap) {
-        const int kz = tap / 9, ky = (tap / 3) % 3, kx = tap % 3;
-        long long so[2] = {0, 0};
-        bool sv[2];
-#pragma unroll
-        for (int r = 0; r < 2; ++r)
-            sv[r] = rv[r] && src_voxel<TRANSPOSED>(a, rn[r], rz[r], ry[r], rx[r], kz, ky, kx, so[r]);
-        if (!__any_sync(0xffffffffu, sv[0] || sv[1])) continue;
-        for (int kc = 0; kc < kchunks; ++kc) {
-            const int c0 = kc * 16 + 2 * t;
-            const uint32_t a0 = load_pair(A, so[0] + c0, sv[0]);
-            const uint32_t a1 = load_pair(A, so[1] + c0, sv[1]);
-            const uint32_t a2 = load_pair(A, so[0] + c0 + 8, sv[0]);
-            const uint32_t a3 = load_pair(A, so[1] + c0 + 8, sv[1]);
-            const bf16* wb = a.B + (long long)tap * a.csrc + c0;
-#pragma unroll
-            for (int j = 0; j < NT; ++j) {
-                const bf16* w = wb + (long long)(8 * j + g) * wstride;
-                const uint32_t b0 = *reinterpret_cast<const uint32_t*>(w);
-                const uint32_t b1 = *reinterpret_cast<const uint32_t*>(w + 8);
-                mma_bf16(acc[j], a0, a1, a2, a3, b0, b1);
-            }
-        }
-    }
-    // epilogue: rows m0 + g (c0, c1) and m0 + g + 8 (c2, c3), channels 8j + 2t, +1
-#pragma unroll
-    for (int r = 0; r < 2; ++r) {
-        if (!rv[r]) continue;
-        const long long m = m0 + g + 8 * r;
-#pragma unroll
-        for (int j = 0; j < NT; ++j) {
-            const int co = 8 * j + 2 * t;
-            float v0 = acc[j][2 * r], v1 = acc[j][2 * r + 1];
-            const long long o = m * a.cdst + co;
-            if (a.bias) {
-                v0 += a.bias[co];
-                v1 += a.bias[co + 1];
-            }
-            if (a.skip) {
-                const __nv_bfloat162 s = *reinterpret_cast<const __nv_bfloat162*>(a.skip + o);
-                v0 += __low2float(s);
-                v1 += __high2float(s);
-            }
-            if (a.relu) {
-                v0 = fmaxf(v0, 0.f);
-                v1 = fmaxf(v1, 0.f);
-            }
-            if constexpr (std::is_same<TO, float>::value) {
-                float2* po = reinterpret_cast<float2*>(reinterpret_cast<float*>(a.out) + o);
-                if (a.accumulate) {
-                    const float2 old = *po;
-                    v0 += old.x;
-                    v1 += old.y;
-                }
-                *po = make_float2(v0, v1);
-            } else {
-                *reinterpret_cast<__nv_bfloat162*>(reinterpret_cast<bf16*>(a.out) + o) = __floats2bfloat162_rn(v0, v1);
-            }
-        }
-    }
+// Eight consecutive channels of the gathered operand as BF16 (16 bytes).
+__device__ __forceinline__ uint4 load8(const bf16* p, long long off) {
+    return *reinterpret_cast<const uint4*>(p + off);
+}
+__device__ __forceinline__ uint4 load8(const float* p, long long off) {
+    const float4 a = *reinterpret_cast<const float4*>(p + off);
+    const float4 b = *reinterpret_cast<const float4*>(p + off + 4);
+    return make_uint4(pack_bf16(a.x, a.y), pack_bf16(a.z, a.w), pack_bf16(b.x, b.y), pack_bf16(b.z, b.w));
 }
 
-// Weight gradient dW[co][tap][ci] += sum over forward-output voxels v of
-// dout[v][co] * in[src(v, tap)][ci].  Block x = (tap, 16-channel block of co),
-// block y = voxel chunk split over 4 warps; a warp covers 16 co x 8*NT ci
-// (NT = cin / 8) and adds its partial sums with atomics.
-template <int NT>
-__global__ void __launch_bounds__(128) k_conv_wgrad(WgradArgs w) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int g = lane >> 2, t = lane & 3;
-    const int cot = blockIdx.x % (w.cout >> 4), tap = blockIdx.x / (w.cout >> 4);
-    const int kz = tap / 9, ky = (tap / 3) % 3, kx = tap % 3;
-    const int co0 = cot * 16;
-    const long long M = w.vout.vox();
-    const long long cb = (long long)blockIdx.y * w.chunk;
-    const long long ce = (cb + w.chunk < M) ? cb + w.chunk : M;
-    const long long per = (((ce - cb) + 63) / 64) * 16;   // 16-voxel steps per warp
-    const long long vb = cb + warp * per, ve = (vb + per < ce) ? vb + per : ce;
-    float acc[NT][4];
+constexpr int kTcRows = 128;        // destination voxels of a block (the MMA's M)
+constexpr int kTcWaitPolls = 1 << 22;   // bounded mbarrier waits (a few hundred ms at most)
+
+// Shared memory of k_conv_tc: two stages of (A: 128 x csrc, B: cdst x csrc) BF16, two mbarriers
+// and the TMEM address slot.
+inline size_t conv_tc_smem(int csrc, int cdst) {
+    return 2 * ((size_t)kTcRows * csrc * 2 + (size_t)cdst * csrc * 2) + 32;
+}
+
+// Implicit-GEMM 3x3x3 convolution on the tcgen05 tensor cores.  A block owns 128
+// destination voxels (one per thread) and all N = cdst destination channels; the FP32
+// accumulator (128 x N) lives in TMEM.  Per tap each thread gathers its voxel's source
+// channels (BF16, zero outside the volume) into the A stage in shared memory, the block
+// copies the tap's weights into the B stage, and one thread issues csrc / 16 MMAs and
+// commits them to the stage's mbarrier; the two stages alternate, so the gather of a
+// tap overlaps the MMAs of the previous one.  The epilogue reads each thread's row
+// back from TMEM (bias, skip, ReLU, store).  Every wait is bounded: on a timeout the
+// block stops issuing, waits (bounded) for what it issued, frees its TMEM, sets *err
+// and returns.
+template <typename TA, typename TO, int N, bool TRANSPOSED>
+__global__ void __launch_bounds__(kTcRows) k_conv_tc(ConvArgs a, int* err) {
+    extern __shared__ __align__(128) uint8_t tsm[];
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int K = a.csrc;
+    const uint32_t abytes = (uint32_t)kTcRows * K * 2, bbytes = (uint32_t)N * K * 2, sbo = (uint32_t)K * 16;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(tsm + 2 * (abytes + bbytes));
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 2);
+    constexpr uint32_t kCols = N <= 32 ? 32 : 64;
+    if (tid == 0) {
+        tc::mbar_init(&bar[0], 1);
+        tc::mbar_init(&bar[1], 1);
+        tc::mbar_init_fence();
+    }
+    if (warp == 0) tc::tmem_alloc(tslot, kCols);
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *tslot;
+
+    const long long M = a.dst.vox();
+    const long long m = (long long)blockIdx.x * kTcRows + tid;
+    const bool rv = m < M;
+    int rn, rz, ry, rx;
+    vox_coords(a.dst, rv ? m : 0, rn, rz, ry, rx);
+    const TA* A = reinterpret_cast<const TA*>(a.A);
+    const int kc8 = K >> 3;
+    constexpr uint32_t idesc = tc::idesc_bf16_f32(kTcRows, N);
+    int issued0 = 0, issued1 = 0;   // commits per stage
+    bool fail = false;
+    for (int tap = 0; tap < 27; ++tap) {
+        const int s = tap & 1;
+        const int iss = s ? issued1 : issued0;
+        if (iss > 0) fail = !tc::mbar_wait(&bar[s], (iss - 1) & 1, kTcWaitPolls);
+        if (__syncthreads_or(fail)) {
+            fail = true;
+            break;
+        }
+        const int kz = tap / 9, ky = (tap / 3) % 3, kx = tap % 3;
+        long long so = 0;
+        const bool sv = rv && src_voxel<TRANSPOSED>(a, rn, rz, ry, rx, kz, ky, kx, so);
+        uint8_t* const sa_p = tsm + s * (abytes + bbytes);
+        uint8_t* arow = sa_p + (tid >> 3) * sbo + (tid & 7) * 16;
+        for (int kc = 0; kc < kc8; ++kc)
+            *reinterpret_cast<uint4*>(arow + kc * 128) = sv ? load8(A, so + 8 * kc) : make_uint4(0, 0, 0, 0);
+        uint8_t* bt = sa_p + abytes;
+        for (int i = tid; i < N * kc8; i += kTcRows) {
+            const int n = i / kc8, kc = i - n * kc8;
+            *reinterpret_cast<uint4*>(bt + (n >> 3) * sbo + kc * 128 + (n & 7) * 16) =
+                *reinterpret_cast<const uint4*>(a.B + ((long long)n * 27 + tap) * K + 8 * kc);
+        }
+        tc::fence_async_shared();
+        __syncthreads();
+        if (tid == 0) {
+            tc::fence_after_sync();
+            const uint32_t sa = tc::smem_u32(sa_p), sb = tc::smem_u32(bt);
+            for (int kc = 0; kc < (K >> 4); ++kc)
+                tc::mma_bf16(tmem, tc::smem_desc(sa + kc * 256, 128, sbo), tc::smem_desc(sb + kc * 256, 128, sbo),
+                             idesc, (tap | kc) != 0);
+            tc::mma_commit(&bar[s]);
+        }
+        if (s) ++issued1; else ++issued0;
+    }
+    // every issued MMA has completed once the last commit of each stage has
+    bool drained = true;
+    if (issued0 > 0) drained = tc::mbar_wait(&bar[0], (issued0 - 1) & 1, kTcWaitPolls) && drained;
+    if (issued1 > 0) drained = tc::mbar_wait(&bar[1], (issued1 - 1) & 1, kTcWaitPolls) && drained;
+    drained = __syncthreads_and(drained);
+    tc::fence_after_sync();
+    if (!fail && drained) {   // block-uniform: the TMEM loads are warp-collective
+        float acc[N];
 #pragma unroll
-    for (int j = 0; j < NT; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
-    for (long long v0 = vb; v0 < ve; v0 += 16) {
-        const long long va[4] = {v0 + 2 * t, v0 + 2 * t + 1, v0 + 2 * t + 8, v0 + 2 * t + 9};
-        long long so[4];
-        bool ok[4];
+        for (int c = 0; c < N; c += 16) tc::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + c, acc + c);
+        const long long o = m * a.cdst;
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            ok[i] = va[i] < ve;
-            so[i] = 0;
-            if (ok[i]) {
-                int n, z, y, x;
-                vox_coords(w.vout, va[i], n, z, y, x);
-                const int sz = z * w.stride + kz - 1, sy = y * w.stride + ky - 1, sx = x * w.stride + kx - 1;
-                const bool in = sz >= 0 && sy >= 0 && sx >= 0 && sz < w.vin.d && sy < w.vin.h && sx < w.vin.w;
-                so[i] = in ? ((((long long)n * w.vin.d + sz) * w.vin.h + sy) * w.vin.w + sx) * w.cin : -1;
+        for (int c = 0; c < N; c += 8) {
+            if (!rv) break;
+            float v[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) v[i] = acc[c + i] + (a.bias ? a.bias[c + i] : 0.f);
+            if (a.skip) {
+                const uint4 sk = *reinterpret_cast<const uint4*>(a.skip + o + c);
+                const __nv_bfloat162* s2 = reinterpret_cast<const __nv_bfloat162*>(&sk);
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    v[2 * i] += __low2float(s2[i]);
+                    v[2 * i + 1] += __high2float(s2[i]);
+                }
+            }
+            if (a.relu) {
+#pragma unroll
+                for (int i = 0; i < 8; ++i) v[i] = fmaxf(v[i], 0.f);
+            }
+            if constexpr (std::is_same<TO, float>::value) {
+                float4* po = reinterpret_cast<float4*>(reinterpret_cast<float*>(a.out) + o + c);
+                if (a.accumulate) {
+                    const float4 p0 = po[0], p1 = po[1];
+                    v[0] += p0.x, v[1] += p0.y, v[2] += p0.z, v[3] += p0.w;
+                    v[4] += p1.x, v[5] += p1.y, v[6] += p1.z, v[7] += p1.w;
+                }
+                po[0] = make_float4(v[0], v[1], v[2], v[3]);
+                po[1] = make_float4(v[4], v[5], v[6], v[7]);
+            } else {
+                *reinterpret_cast<uint4*>(reinterpret_cast<bf16*>(a.out) + o + c) =
+                    make_uint4(pack_bf16(v[0], v[1]), pack_bf16(v[2], v[3]), pack_bf16(v[4], v[5]), pack_bf16(v[6], v[7]));
             }
         }
-        auto dv = [&](int i, int co) { return ok[i] ? w.dout[va[i] * w.cout + co] : 0.f; };
-        const uint32_t a0 = pack_bf16(dv(0, co0 + g), dv(1, co0 + g));
-        const uint32_t a1 = pack_bf16(dv(0, co0 + g + 8), dv(1, co0 + g + 8));
-        const uint32_t a2 = pack_bf16(dv(2, co0 + g), dv(3, co0 + g));
-        const uint32_t a3 = pack_bf16(dv(2, co0 + g + 8), dv(3, co0 + g + 8));
-        auto iv = [&](int i, int ci) {
-            return (ok[i] && so[i] >= 0) ? w.in[so[i] + ci] : __float2bfloat16(0.f);
-        };
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) {
+        tc::fence_after_sync();
+        tc::tmem_dealloc(tmem, kCols);
+    }
+    if (tid == 0 && (fail || !drained)) atomicExch(err, 1);
+}
+
+constexpr int kWgVox = 64;   // voxels per stage of k_wgrad_tc (four K = 16 MMAs)
+
+inline size_t wgrad_tc_smem(int cout) { return 2 * ((size_t)kTcRows * kWgVox * 2 + (size_t)cout * kWgVox * 2) + 32; }
+
+// Weight gradient on the tcgen05 tensor cores: dW[co][tap][ci] += sum over forward-output
+// voxels v of dout[v][co] * in[src(v, tap)][ci].  MMA rows are 128 consecutive (tap, ci)
+// pairs of the 27 * cin (block x), columns the N = cout output channels, the reduction runs
+// over the block's voxel range (block y) 64 voxels per stage.  Both operands are written
+// K-major (voxels contiguous inside a core matrix) by the threads: a thread owns one voxel
+// of the stage and scatters its 8-channel groups down the rows.  The FP32 accumulator
+// stays in TMEM until the end, then every thread adds its row to dW with atomics.  Waits
+// are bounded as in k_conv_tc.
+template <int N>
+__global__ void __launch_bounds__(kTcRows) k_wgrad_tc(WgradArgs w, int* err) {
+    extern __shared__ __align__(128) uint8_t tsm[];
+    const int tid = threadIdx.x, warp = tid >> 5;
+    constexpr uint32_t abytes = kTcRows * kWgVox * 2, bbytes = N * kWgVox * 2, sbo = kWgVox * 16;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(tsm + 2 * (abytes + bbytes));
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 2);
+    constexpr uint32_t kCols = N <= 32 ? 32 : 64;
+    if (tid == 0) {
+        tc::mbar_init(&bar[0], 1);
+        tc::mbar_init(&bar[1], 1);
+        tc::mbar_init_fence();
+    }
+    if (warp == 0) tc::tmem_alloc(tslot, kCols);
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *tslot;
+
+    const int rows = 27 * w.cin;
+    const int r0 = blockIdx.x * kTcRows;   // first (tap, ci) row of the block
+    const long long M = w.vout.vox();
+    const long long cb = (long long)blockIdx.y * w.chunk;
+    const long long ce = cb + w.chunk < M ? cb + w.chunk : M;
+    const int nst = (int)((ce - cb + kWgVox - 1) / kWgVox);
+    const int vl = tid & (kWgVox - 1), gh = tid / kWgVox;   // voxel of the stage, half of the row groups
+    constexpr uint32_t idesc = tc::idesc_bf16_f32(kTcRows, N);
+    int issued0 = 0, issued1 = 0;
+    bool fail = false;
+    for (int it = 0; it < nst; ++it) {
+        const int s = it & 1;
+        const int iss = s ? issued1 : issued0;
+        if (iss > 0) fail = !tc::mbar_wait(&bar[s], (iss - 1) & 1, kTcWaitPolls);
+        if (__syncthreads_or(fail)) {
+            fail = true;
+            break;
+        }
+        uint8_t* const sa_p = tsm + s * (abytes + bbytes);
+        uint8_t* const sb_p = sa_p + abytes;
+        const long long v = cb + (long long)it * kWgVox + vl;
+        const bool vok = v < ce;
+        int n = 0, z = 0, y = 0, x = 0;
+        if (vok) vox_coords(w.vout, v, n, z, y, x);
+        const uint32_t col = (vl >> 3) * 128 + (vl & 7) * 2;   // this voxel's column in a core matrix row group
+        // A: 16 groups of 8 rows (tap, ci..ci+7); this thread fills 8 of them for its voxel
+#pragma unroll 2
+        for (int g = gh; g < kTcRows / 8; g += kTcRows / kWgVox) {
+            const int r = r0 + 8 * g;
+            uint4 val = make_uint4(0, 0, 0, 0);
+            if (vok && r < rows) {
+                const int tap = r / w.cin, ci = r - tap * w.cin;
+                const int kz = tap / 9, ky = (tap / 3) % 3, kx = tap % 3;
+                const int sz = z * w.stride + kz - 1, sy = y * w.stride + ky - 1, sx = x * w.stride + kx - 1;
+                if (sz >= 0 && sy >= 0 && sx >= 0 && sz < w.vin.d && sy < w.vin.h && sx < w.vin.w)
+                    val = *reinterpret_cast<const uint4*>(
+                        w.in + ((((long long)n * w.vin.d + sz) * w.vin.h + sy) * w.vin.w + sx) * w.cin + ci);
+            }
+            const uint16_t* h = reinterpret_cast<const uint16_t*>(&val);
+            uint8_t* dst = sa_p + g * sbo + col;
 #pragma unroll
-        for (int j = 0; j < NT; ++j) {
-            const int ci = 8 * j + g;
-            __nv_bfloat162 p0, p1;
-            p0.x = iv(0, ci);
-            p0.y = iv(1, ci);
-            p1.x = iv(2, ci);
-            p1.y = iv(3, ci);
-            mma_bf16(acc[j], a0, a1, a2, a3, *reinterpret_cast<uint32_t*>(&p0), *reinterpret_cast<uint32_t*>(&p1));
+            for (int i = 0; i < 8; ++i) *reinterpret_cast<uint16_t*>(dst + i * 16) = h[i];
+        }
+        // B: N / 8 groups of 8 output channels of dout (FP32 -> BF16)
+        for (int g = gh; g < N / 8; g += kTcRows / kWgVox) {
+            float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
+            if (vok) {
+                const float4* src = reinterpret_cast<const float4*>(w.dout + v * w.cout + 8 * g);
+                a = src[0];
+                b = src[1];
+            }
+            const bf16 hv[8] = {__float2bfloat16(a.x), __float2bfloat16(a.y), __float2bfloat16(a.z),
+                                __float2bfloat16(a.w), __float2bfloat16(b.x), __float2bfloat16(b.y),
+                                __float2bfloat16(b.z), __float2bfloat16(b.w)};
+            uint8_t* dst = sb_p + g * sbo + col;
+#pragma unroll
+            for (int i = 0; i < 8; ++i) *reinterpret_cast<bf16*>(dst + i * 16) = hv[i];
+        }
+        tc::fence_async_shared();
+        __syncthreads();
+        if (tid == 0) {
+            tc::fence_after_sync();
+            const uint32_t sa = tc::smem_u32(sa_p), sb = tc::smem_u32(sb_p);
+#pragma unroll
+            for (int kc = 0; kc < kWgVox / 16; ++kc)
+                tc::mma_bf16(tmem, tc::smem_desc(sa + kc * 256, 128, sbo), tc::smem_desc(sb + kc * 256, 128, sbo),
+                             idesc, (it | kc) != 0);
+            tc::mma_commit(&bar[s]);
+        }
+        if (s) ++issued1; else ++issued0;
+    }
+    bool drained = true;
+    if (issued0 > 0) drained = tc::mbar_wait(&bar[0], (issued0 - 1) & 1, kTcWaitPolls) && drained;
+    if (issued1 > 0) drained = tc::mbar_wait(&bar[1], (issued1 - 1) & 1, kTcWaitPolls) && drained;
+    drained = __syncthreads_and(drained);
+    tc::fence_after_sync();
+    if (!fail && drained && nst > 0) {   // block-uniform: the TMEM loads are warp-collective
+        float acc[N];
+#pragma unroll
+        for (int c = 0; c < N; c += 16) tc::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + c, acc + c);
+        const int r = r0 + tid;
+        if (r < rows) {
+            const int tap = r / w.cin, ci = r - tap * w.cin;
+#pragma unroll
+            for (int co = 0; co < N; ++co) atomicAdd(w.dw + ((long long)co * 27 + tap) * w.cin + ci, acc[co]);
         }
     }
-#pragma unroll
-    for (int j = 0; j < NT; ++j) {
-        const int ci = 8 * j + 2 * t;
-        float* d0 = w.dw + ((long long)(co0 + g) * 27 + tap) * w.cin + ci;
-        float* d1 = w.dw + ((long long)(co0 + g + 8) * 27 + tap) * w.cin + ci;
-        atomicAdd(d0, acc[j][0]);
-        atomicAdd(d0 + 1, acc[j][1]);
-        atomicAdd(d1, acc[j][2]);
-        atomicAdd(d1 + 1, acc[j][3]);
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) {
+        tc::fence_after_sync();
+        tc::tmem_dealloc(tmem, kCols);
     }
+    if (tid == 0 && (fail || !drained)) atomicExch(err, 1);
 }
 
 // bias gradient: db[c] += sum_v g[v][c]
@@ -421,6 +528,7 @@ struct tog_nn {
     float *gy = nullptr, *g0 = nullptr, *g0b = nullptr, *gu0 = nullptr, *g1 = nullptr, *g1b = nullptr, *gu1 = nullptr;
     float *g2 = nullptr, *g2b = nullptr, *gu2 = nullptr, *g3 = nullptr;
     double* d_loss = nullptr;
+    int* d_err = nullptr;           // set by a tensor-core kernel whose mbarrier wait timed out
     std::vector<void*> allocs;
     cudaStream_t stream = nullptr;
     int steps = 0;
@@ -442,15 +550,30 @@ int ew_grid(const tog_nn* nn, long long n) {
 }
 
 template <typename TA, typename TO, bool TR>
-void conv_launch(const ConvArgs& a, cudaStream_t s) {
+void conv_launch(const tog_nn* nn, const ConvArgs& a, cudaStream_t s) {
     const long long M = a.dst.vox();
-    const int grid = (int)((M + 63) / 64);
-    switch (a.cdst / 8) {
-        case 2: k_conv<TA, TO, 2, TR><<<grid, 128, 0, s>>>(a); break;
-        case 4: k_conv<TA, TO, 4, TR><<<grid, 128, 0, s>>>(a); break;
-        case 6: k_conv<TA, TO, 6, TR><<<grid, 128, 0, s>>>(a); break;
-        default: k_conv<TA, TO, 8, TR><<<grid, 128, 0, s>>>(a); break;
+    const int grid = (int)((M + kTcRows - 1) / kTcRows);
+    const size_t sm = conv_tc_smem(a.csrc, a.cdst);
+    switch (a.cdst / 16) {
+        case 1: k_conv_tc<TA, TO, 16, TR><<<grid, kTcRows, sm, s>>>(a, nn->d_err); break;
+        case 2: k_conv_tc<TA, TO, 32, TR><<<grid, kTcRows, sm, s>>>(a, nn->d_err); break;
+        case 3: k_conv_tc<TA, TO, 48, TR><<<grid, kTcRows, sm, s>>>(a, nn->d_err); break;
+        default: k_conv_tc<TA, TO, 64, TR><<<grid, kTcRows, sm, s>>>(a, nn->d_err); break;
     }
+}
+
+// the tcgen05 kernels take more than the default 48 KB of dynamic shared memory
+template <typename TA, typename TO, bool TR>
+cudaError_t conv_tc_attributes() {
+    const int sm = (int)conv_tc_smem(64, 64);
+    cudaError_t e = cudaFuncSetAttribute(k_conv_tc<TA, TO, 16, TR>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_conv_tc<TA, TO, 32, TR>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_conv_tc<TA, TO, 48, TR>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_conv_tc<TA, TO, 64, TR>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    return e;
 }
 
 // forward convolution of layer l from `in` (vol vi) to `out` (vol vo)
@@ -469,7 +592,7 @@ void conv_fwd(tog_nn* nn, int l, const bf16* in, Vol vi, void* out, Vol vo, cons
     a.csrc = C.cin;
     a.cdst = C.cout;
     a.stride = C.stride;
-    conv_launch<bf16, TO, false>(a, nn->stream);
+    conv_launch<bf16, TO, false>(nn, a, nn->stream);
 }
 
 // input gradient of layer l: gin (vol vi, cin) (+)= conv^T(gout (vol vo, cout))
@@ -485,7 +608,7 @@ void conv_bwd_data(tog_nn* nn, int l, const float* gout, Vol vo, float* gin, Vol
     a.csrc = C.cout;
     a.cdst = C.cin;
     a.stride = C.stride;
-    conv_launch<float, float, true>(a, nn->stream);
+    conv_launch<float, float, true>(nn, a, nn->stream);
 }
 
 void conv_wgrad(tog_nn* nn, int l, const float* gout, Vol vo, const bf16* in, Vol vi) {
@@ -500,14 +623,16 @@ void conv_wgrad(tog_nn* nn, int l, const float* gout, Vol vo, const bf16* in, Vo
     w.cout = C.cout;
     w.stride = C.stride;
     const long long M = vo.vox();
-    const long long want = std::max<long long>(1, (long long)nn->nsm * 8 / (27 * (C.cout / 16)));
-    w.chunk = std::max<long long>(64, ((M + want - 1) / want + 63) / 64 * 64);
-    dim3 grid(27 * (C.cout / 16), (unsigned)((M + w.chunk - 1) / w.chunk));
-    switch (C.cin / 8) {
-        case 2: k_conv_wgrad<2><<<grid, 128, 0, nn->stream>>>(w); break;
-        case 4: k_conv_wgrad<4><<<grid, 128, 0, nn->stream>>>(w); break;
-        case 6: k_conv_wgrad<6><<<grid, 128, 0, nn->stream>>>(w); break;
-        default: k_conv_wgrad<8><<<grid, 128, 0, nn->stream>>>(w); break;
+    const int gx = (27 * C.cin + kTcRows - 1) / kTcRows;
+    const long long want = std::max<long long>(1, (long long)nn->nsm * 4 / gx);
+    w.chunk = std::max<long long>(kWgVox, ((M + want - 1) / want + kWgVox - 1) / kWgVox * kWgVox);
+    dim3 grid(gx, (unsigned)((M + w.chunk - 1) / w.chunk));
+    const size_t sm = wgrad_tc_smem(C.cout);
+    switch (C.cout / 16) {
+        case 1: k_wgrad_tc<16><<<grid, kTcRows, sm, nn->stream>>>(w, nn->d_err); break;
+        case 2: k_wgrad_tc<32><<<grid, kTcRows, sm, nn->stream>>>(w, nn->d_err); break;
+        case 3: k_wgrad_tc<48><<<grid, kTcRows, sm, nn->stream>>>(w, nn->d_err); break;
+        default: k_wgrad_tc<64><<<grid, kTcRows, sm, nn->stream>>>(w, nn->d_err); break;
     }
     k_bias_grad<<<ew_grid(nn, M * C.cout), 256, C.cout * sizeof(float), nn->stream>>>(gout, nn->d_g + C.boff, M,
                                                                                       C.cout);
@@ -604,6 +729,14 @@ int nn_forward_dev(tog_nn* nn, const float* in_dev, float* out_dev, cudaStream_t
     return TOG_OK;
 }
 
+int nn_status(tog_nn* nn, cudaStream_t stream) {
+    int flag = 0;
+    NN_CUDA(cudaMemcpyAsync(&flag, nn->d_err, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    NN_CUDA(cudaStreamSynchronize(stream));
+    if (flag) return nn_fail(TOG_ERR_CUDA, "warm-start network: a tensor-core convolution timed out waiting for its MMAs");
+    return TOG_OK;
+}
+
 bool nn_matches(const tog_nn* nn, const int nodes[3], int batch) {
     return nn && nn->nodes[0] == nodes[0] && nn->nodes[1] == nodes[1] && nn->nodes[2] == nodes[2] &&
            nn->lv[0].n == batch;
@@ -668,6 +801,18 @@ int tog_nn_create(const int32_t nodes[3], int32_t batch, uint64_t seed, tog_nn**
     R(nalloc(nn, &nn->gu2, n2 * 64));
     R(nalloc(nn, &nn->g3, n3 * 64));
     R(nalloc(nn, &nn->d_loss, 1));
+    R(nalloc(nn, &nn->d_err, 1));
+    if (rc == TOG_OK) {
+        cudaError_t e = conv_tc_attributes<bf16, bf16, false>();
+        if (e == cudaSuccess) e = conv_tc_attributes<bf16, float, false>();
+        if (e == cudaSuccess) e = conv_tc_attributes<float, float, true>();
+        const int wsm = (int)wgrad_tc_smem(64);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_wgrad_tc<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, wsm);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_wgrad_tc<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, wsm);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_wgrad_tc<48>, cudaFuncAttributeMaxDynamicSharedMemorySize, wsm);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_wgrad_tc<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, wsm);
+        if (e != cudaSuccess) rc = nn_fail(TOG_ERR_CUDA, std::string("tog_nn_create: ") + cudaGetErrorString(e));
+    }
     if (rc != TOG_OK) {
         std::string m = tog_last_error();
         tog_nn_destroy(nn);
@@ -690,6 +835,7 @@ int tog_nn_create(const int32_t nodes[3], int32_t batch, uint64_t seed, tog_nn**
     }
     cudaError_t e = cudaMemcpy(nn->d_p, h.data(), off * sizeof(float), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemset(nn->d_m, 0, off * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemset(nn->d_err, 0, sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(nn->d_v, 0, off * sizeof(float));
     if (e == cudaSuccess) {
         refresh_bf16(nn);
@@ -743,7 +889,8 @@ int tog_nn_set_params(tog_nn* nn, const float* params) {
 
 int tog_nn_forward(tog_nn* nn, const float* in_dev, float* out_dev) {
     if (!nn || !in_dev || !out_dev) return nn_fail(TOG_ERR_ARG, "null argument");
-    return nn_forward_dev(nn, in_dev, out_dev, nn->stream);
+    const int rc = nn_forward_dev(nn, in_dev, out_dev, nn->stream);
+    return rc != TOG_OK ? rc : nn_status(nn, nn->stream);
 }
 
 int tog_nn_gradients(tog_nn* nn, const float* in_dev, const float* target_dev, double* loss, float* grads) {
@@ -752,6 +899,7 @@ int tog_nn_gradients(tog_nn* nn, const float* in_dev, const float* target_dev, d
     double l = 0.0;
     int rc = backward(nn, target_dev, &l);
     if (rc != TOG_OK) return rc;
+    if ((rc = nn_status(nn, nn->stream)) != TOG_OK) return rc;
     if (loss) *loss = l;
     if (grads) {
         NN_CUDA(cudaMemcpyAsync(grads, nn->d_g, nn->nparam * sizeof(float), cudaMemcpyDeviceToHost, nn->stream));
@@ -772,7 +920,7 @@ int tog_nn_train_step(tog_nn* nn, const float* in_dev, const float* target_dev, 
                                                             1e-8f, c1, c2);
     refresh_bf16(nn);
     NN_CUDA(cudaGetLastError());
-    return TOG_OK;
+    return loss ? nn_status(nn, nn->stream) : TOG_OK;
 }
 
 }  // extern "C"

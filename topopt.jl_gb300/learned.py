@@ -111,6 +111,42 @@ def evaluate(nels, run, steps, net=None, rmin=1.5, rtol=1e-8, modes=("cold", "pr
     return out
 
 
+def start_quality_bound(nels, run, k=8, thetas=(0.0, 0.5, 0.9, 0.99, 0.999), rmin=1.5, rtol=1e-8):
+    """What any predicted start can save at most.  After k design iterations of the run,
+    the solve of iteration k + 1 (densities rho, previous solution u_prev, exact solution
+    u* = the FP64 solve to rtol 1e-13) is repeated from u_prev + theta (u* - u_prev) for
+    every theta, i.e. from a prediction that removes the fraction theta of the error of
+    the previous-step start (theta = 0), and from a cold start.  Returns the inner PCG
+    iterations of FP32-IR to rtol (relative to ||f||) and the relative energy-norm error
+    ||u0 - u*||_K / ||u*||_K of each start."""
+    s, loop = make_loop(nels, run, rmin, rtol, True)
+    for _ in range(k):
+        loop.step()
+    u_prev = s.u
+    loop.step()
+    rho = loop.physical
+    s.close()
+    prob = api.LoadedCantilever(nels, (1.0, 1.0, 1.0), run["node"], run["direction"])
+    t = api.FEASolver(api.GB300Solver, prob, xmin=1e-9, penalty=api.PowerPenaltyFun(3.0), rtol=1e-13, abstol=0.0,
+                      cg_max_iter=400000, precision="fp64", warm_start=True)
+    t.vars = rho
+    t.u = u_prev
+    t()
+    ustar = t.u
+    t.rtol = rtol
+    kstar = float(ustar @ t.matvec(ustar))
+    out = {"design_iteration": k + 1, "rtol": rtol, "starts": []}
+    for name, u0 in [("cold", np.zeros_like(ustar))] + [("theta=%g" % th, u_prev + th * (ustar - u_prev))
+                                                        for th in thetas]:
+        e = u0 - ustar
+        t.u = u0
+        t(precision="fp32_ir", warm_start=True)
+        out["starts"].append({"start": name, "pcg_iters": int(t.last_stats.iterations),
+                              "energy_error": float(np.sqrt(max(e @ t.matvec(e), 0.0) / kstar))})
+    t.close()
+    return out
+
+
 def main(argv=None):
     """Train the warm-start network for one grid and evaluate it:
         python -m topopt_gb300.learned --nels 96,48,48 --runs 40 --steps 26 --epochs 8 \\
