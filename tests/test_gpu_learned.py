@@ -34,3 +34,20 @@ def test_learned_warm_start_trains_and_keeps_the_trajectory(tg):
           "learned / previous = %.3f (below 1 would be a gain)" % (its["learned"] / its["previous"]))
     assert all(np.isfinite(v) and v > 0 for v in its.values())
     net.close()
+
+
+def test_start_quality_bound_scales_the_error(tg):
+    """The bound's starts are u_prev + theta (u* - u_prev): their energy-norm errors are
+    (1 - theta) times the previous-step start's, and a start 1000x closer than the
+    previous solution needs fewer PCG iterations than it."""
+    from topopt_gb300 import learned as LW
+    nels = (32, 16, 16)
+    run = LW.sample_runs(1, nels, seed=5)[0]
+    r = LW.start_quality_bound(nels, run, k=3)
+    st = {s["start"]: s for s in r["starts"]}
+    e0 = st["theta=0"]["energy_error"]
+    assert 0 < e0 < 1
+    for th in (0.5, 0.9, 0.99, 0.999):
+        assert abs(st["theta=%g" % th]["energy_error"] - (1 - th) * e0) <= 1e-6 * e0, th
+    assert st["theta=0.999"]["pcg_iters"] < st["theta=0"]["pcg_iters"]
+    print({k: v["pcg_iters"] for k, v in st.items()})
