@@ -358,7 +358,9 @@ def run_ours(args):
     if args.no_extra:
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "unit": "design_iters/s", "steps": args.steps,
-                              "warmup": args.warmup, "partial": "e2e/fp64/roofline legs skipped (--no-extra)",
+                              "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps,
+                              "gpu_launches": int(launches), "clocks": clocks,
+                              "partial": "e2e/fp64/roofline legs skipped (--no-extra)",
                               "inner_cg_iters_per_step": [int(s.cg_iterations) for s in stats]}), flush=True)
         return 0
 

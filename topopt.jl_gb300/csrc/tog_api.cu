@@ -50,6 +50,12 @@ int fail(int code, const std::string& msg) {
 
 constexpr int kEwThreads = 256;
 constexpr int kOcMaxSteps = 100;
+// Iterations per pass of a device loop's WHILE body.  Every pass of a conditional node
+// costs about 3 us of scheduling, 5% of a 56 us PCG iteration at 160x80x80; a body of
+// several iterations pays it once per pass.  Kernels that find the state done return at
+// once, so a pass that ends early costs those launches only.
+constexpr int kPcgUnroll = 16;
+constexpr int kOcUnroll = 4;
 
 }  // namespace
 
@@ -162,7 +168,8 @@ struct tog_handle {
     cudaGraphExec_t g_pcg64 = nullptr, g_pcg32 = nullptr, g_oc = nullptr;
     cudaGraphExec_t g_pcg64e = nullptr;   // FP64 batch with the EnergyCriteria check
     int conv = TOG_CONV_DEFAULT;
-    int graph_nodes64 = 0, graph_nodes32 = 0;
+    int graph_nodes64 = 0, graph_nodes32 = 0;   // kernels per PCG iteration in the loop body
+    int pcg_unroll = kPcgUnroll;                 // PCG iterations per pass of the body (TOG_PCG_UNROLL)
 
     Dims dims() const {
         Dims D;
@@ -452,16 +459,20 @@ int build_pcg_graph(tog_handle* h, cudaGraphExec_t* out, bool energy = false) {
     cudaGraph_t body = cp.conditional.phGraph_out[0];
     TOG_CUDA(cudaStreamBeginCaptureToGraph(h->own, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
     const long long before = g_launches.load();
-    launch_matvec<T, MV_PCG>(h, h->own, nullptr, nullptr, nullptr);
-    launch_pcg_update<T>(h, h->own, LoopCond{ch, 1});
-    if (energy) {
-        k_energy_check<<<h->ew_blocks(h->ndofs), kEwThreads, 0, h->own>>>(h->d_u, h->d_r64, h->d_f, h->ndofs,
-                                                                         h->d_st64, h->d_partials);
-        TOG_LAUNCHED(1);
+    const int U = h->pcg_unroll;
+    for (int k = 0; k < U; ++k) {   // only the body's last update sets the loop condition
+        launch_matvec<T, MV_PCG>(h, h->own, nullptr, nullptr, nullptr);
+        launch_pcg_update<T>(h, h->own, LoopCond{ch, k == U - 1 ? 1 : 0});
+        if (energy) {
+            k_energy_check<<<h->ew_blocks(h->ndofs), kEwThreads, 0, h->own>>>(h->d_u, h->d_r64, h->d_f, h->ndofs,
+                                                                             h->d_st64, h->d_partials);
+            TOG_LAUNCHED(1);
+        }
     }
     // kernels per iteration; captured launches run only when the graph is launched
-    const int nodes = (int)(g_launches.load() - before);
-    g_launches.fetch_sub(nodes);
+    const long long captured = g_launches.load() - before;
+    g_launches.fetch_sub(captured);
+    const int nodes = (int)(captured / U);
     (std::is_same<T, double>::value ? h->graph_nodes64 : h->graph_nodes32) = nodes;
     cudaGraph_t cap = nullptr;
     TOG_CUDA(cudaStreamEndCapture(h->own, &cap));
@@ -488,9 +499,11 @@ int run_pcg(tog_handle* h, bool energy = false) {
     if (h->h_st->done) return TOG_OK;
     TOG_CUDA(cudaGraphLaunch(*g, h->stream));
     TOG_TRY(sync_state(h, d_st));
-    // launches of this segment: the condition kernel and the body of every iteration run
-    // (plus at most one body that found the state done)
-    TOG_LAUNCHED(1 + (long long)(h->h_st->it - it0 + 1) *
+    // launches of this segment: the condition kernel and every pass of the body (the last
+    // one may end early: its remaining kernels find the state done and return; one more
+    // pass when an EnergyCriteria check ended the loop after the body's last update)
+    const long long passes = (h->h_st->it - it0 + h->pcg_unroll - 1) / h->pcg_unroll + (energy ? 1 : 0);
+    TOG_LAUNCHED(1 + std::max(1LL, passes) * h->pcg_unroll *
                          (std::is_same<T, double>::value ? h->graph_nodes64 : h->graph_nodes32));
     return TOG_OK;
 }
@@ -954,8 +967,9 @@ int build_oc_graph(tog_handle* h) {
     const int nb = h->ew_blocks(h->ncells);
     TOG_CUDA(cudaStreamBeginCaptureToGraph(h->own, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
                                            cudaStreamCaptureModeThreadLocal));
-    k_oc_step<<<nb, kEwThreads, 0, h->own>>>(h->d_x, h->d_B, h->d_w, h->ncells, h->d_oc, h->d_partials, h->d_fpos,
-                                             LoopCond{ch, 1});
+    for (int k = 0; k < kOcUnroll; ++k)   // only the body's last step sets the loop condition
+        k_oc_step<<<nb, kEwThreads, 0, h->own>>>(h->d_x, h->d_B, h->d_w, h->ncells, h->d_oc, h->d_partials,
+                                                 h->d_fpos, LoopCond{ch, k == kOcUnroll - 1 ? 1 : 0});
     cudaGraph_t body = nullptr;
     TOG_CUDA(cudaStreamEndCapture(h->own, &body));
     TOG_CUDA(cudaStreamBeginCaptureToGraph(h->own, g, &loop, nullptr, 1, cudaStreamCaptureModeThreadLocal));
@@ -979,7 +993,8 @@ int oc_dev(tog_handle* h, double volfrac, double move) {
     TOG_CUDA(cudaGraphLaunch(h->g_oc, h->stream));
     TOG_CUDA(cudaMemcpyAsync(h->h_oc, h->d_oc, sizeof(OcState), cudaMemcpyDeviceToHost, h->stream));
     TOG_CUDA(cudaStreamSynchronize(h->stream));
-    TOG_LAUNCHED(2 + h->h_oc->steps);   // condition, every bisection step, final
+    // condition, every pass of the body (the last may end early), final
+    TOG_LAUNCHED(2 + (long long)std::max(1, (h->h_oc->steps + kOcUnroll - 1) / kOcUnroll) * kOcUnroll);
     return TOG_OK;
 }
 
@@ -1193,6 +1208,7 @@ int tog_create(const tog_problem_desc* desc, tog_handle** out) {
     h->stream = h->own;
     if (const char* e = std::getenv("TOG_RU_DELTA")) h->ru_delta = std::min(0.9, std::max(1e-6, std::atof(e)));
     if (const char* e = std::getenv("TOG_UPD_BLOCKS_PER_SM")) h->upd_per_sm = std::min(32, std::max(1, std::atoi(e)));
+    if (const char* e = std::getenv("TOG_PCG_UNROLL")) h->pcg_unroll = std::min(32, std::max(1, std::atoi(e)));
     if (dim == 3) {
         // z-chunk length: minimise (rounds of resident blocks) x (layers + prologue)
         h->nt[0] = (h->nel[0] + 31) / 32;
