@@ -121,7 +121,6 @@ __device__ __forceinline__ uint4 load8(const float* p, long long off) {
 }
 
 constexpr int kTcRows = 128;        // destination voxels of a block (the MMA's M)
-constexpr int kTcWaitPolls = 1 << 22;   // bounded mbarrier waits (a few hundred ms at most)
 
 // Shared memory of k_conv_tc: two stages of (A: 128 x csrc, B: cdst x csrc) BF16, two mbarriers
 // and the TMEM address slot.
@@ -172,7 +171,7 @@ __global__ void __launch_bounds__(kTcRows) k_conv_tc(ConvArgs a, int* err) {
     for (int tap = 0; tap < 27; ++tap) {
         const int s = tap & 1;
         const int iss = s ? issued1 : issued0;
-        if (iss > 0) fail = !tc::mbar_wait(&bar[s], (iss - 1) & 1, kTcWaitPolls);
+        if (iss > 0) fail = !tc::mbar_wait(&bar[s], (iss - 1) & 1, tc::kTcWaitPolls);
         if (__syncthreads_or(fail)) {
             fail = true;
             break;
@@ -204,8 +203,8 @@ __global__ void __launch_bounds__(kTcRows) k_conv_tc(ConvArgs a, int* err) {
     }
     // every issued MMA has completed once the last commit of each stage has
     bool drained = true;
-    if (issued0 > 0) drained = tc::mbar_wait(&bar[0], (issued0 - 1) & 1, kTcWaitPolls) && drained;
-    if (issued1 > 0) drained = tc::mbar_wait(&bar[1], (issued1 - 1) & 1, kTcWaitPolls) && drained;
+    if (issued0 > 0) drained = tc::mbar_wait(&bar[0], (issued0 - 1) & 1, tc::kTcWaitPolls) && drained;
+    if (issued1 > 0) drained = tc::mbar_wait(&bar[1], (issued1 - 1) & 1, tc::kTcWaitPolls) && drained;
     drained = __syncthreads_and(drained);
     tc::fence_after_sync();
     if (!fail && drained) {   // block-uniform: the TMEM loads are warp-collective
@@ -300,7 +299,7 @@ __global__ void __launch_bounds__(kTcRows) k_wgrad_tc(WgradArgs w, int* err) {
     for (int it = 0; it < nst; ++it) {
         const int s = it & 1;
         const int iss = s ? issued1 : issued0;
-        if (iss > 0) fail = !tc::mbar_wait(&bar[s], (iss - 1) & 1, kTcWaitPolls);
+        if (iss > 0) fail = !tc::mbar_wait(&bar[s], (iss - 1) & 1, tc::kTcWaitPolls);
         if (__syncthreads_or(fail)) {
             fail = true;
             break;
@@ -359,8 +358,8 @@ __global__ void __launch_bounds__(kTcRows) k_wgrad_tc(WgradArgs w, int* err) {
         if (s) ++issued1; else ++issued0;
     }
     bool drained = true;
-    if (issued0 > 0) drained = tc::mbar_wait(&bar[0], (issued0 - 1) & 1, kTcWaitPolls) && drained;
-    if (issued1 > 0) drained = tc::mbar_wait(&bar[1], (issued1 - 1) & 1, kTcWaitPolls) && drained;
+    if (issued0 > 0) drained = tc::mbar_wait(&bar[0], (issued0 - 1) & 1, tc::kTcWaitPolls) && drained;
+    if (issued1 > 0) drained = tc::mbar_wait(&bar[1], (issued1 - 1) & 1, tc::kTcWaitPolls) && drained;
     drained = __syncthreads_and(drained);
     tc::fence_after_sync();
     if (!fail && drained && nst > 0) {   // block-uniform: the TMEM loads are warp-collective

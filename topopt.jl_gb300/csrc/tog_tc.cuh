@@ -18,6 +18,8 @@
 namespace tog {
 namespace tc {
 
+constexpr int kTcWaitPolls = 1 << 22;   // bound of an mbarrier wait (a few hundred ms at most)
+
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
 // Shared memory matrix descriptor: start address, leading (K) and stride (8-row)
