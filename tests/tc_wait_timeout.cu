@@ -22,9 +22,7 @@ __global__ void k_wait(int arrive, int limit, int* out) {
     __syncthreads();
     tc::fence_after_sync();
     if (arrive && tid == 0) {
-        uint64_t state;
-        asm volatile("mbarrier.arrive.shared::cta.b64 %0, [%1];" : "=l"(state) : "r"(tc::smem_u32(&bar)) : "memory");
-        (void)state;
+        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc::smem_u32(&bar)) : "memory");
     }
     const bool done = tc::mbar_wait(&bar, 0, limit);
     const bool all = __syncthreads_and(done);
