@@ -57,14 +57,15 @@ __global__ void __launch_bounds__(32 * kM3Warps) k_march3(const Mv3Args<float> A
     const float* __restrict__ pold = (it & 1) ? A.P0 : A.P1;
     const float beta = (float)st->beta;
     const int lane = threadIdx.x & 31;
-    const long long GW = (long long)gridDim.x * kM3Warps;
-    const long long gw = (long long)blockIdx.x * kM3Warps + (threadIdx.x >> 5);
+    // 32-bit index arithmetic: the handle keeps 3 x nodes below 2^31
+    const int GW = gridDim.x * kM3Warps;
+    const int gw = blockIdx.x * kM3Warps + (threadIdx.x >> 5);
     const int nnx = A.nn[0], nny = A.nn[1], nnz = A.nn[2], nelx = A.nel[0], nely = A.nel[1], nelz = A.nel[2];
-    const long long plane = (long long)nnx * nny;
-    const long long items = (long long)nstrip * nny * nband;   // (column, z band), band fastest
+    const unsigned plane = (unsigned)nnx * (unsigned)nny;
+    const int items = nstrip * nny * nband;   // (column, z band), band fastest
     float dot = 0.f;
-    for (long long t = gw; t < items; t += GW) {
-        const long long col = t / nband;
+    for (int t = gw; t < items; t += GW) {
+        const int col = t / nband;
         const int band = (int)(t - col * nband);
         const int za = band * lzb;
         const int zb = za + lzb < nnz ? za + lzb : nnz;
@@ -78,13 +79,13 @@ __global__ void __launch_bounds__(32 * kM3Warps) k_march3(const Mv3Args<float> A
         bool rok[3];
 #pragma unroll
         for (int r = 0; r < 3; ++r) rok[r] = colok && y - 1 + r >= 0 && y - 1 + r < nny;
-        const long long nb = x + (long long)nnx * (y - 1);   // node (x, y - 1, 0)
+        const unsigned xu = (unsigned)x;   // used only where the node exists (x >= 0)
         auto load = [&](int j, M3Plane& R) {
             const bool pok = j >= 0 && j < nnz;
 #pragma unroll
             for (int r = 0; r < 3; ++r) {
                 const bool ok = rok[r] && pok;
-                const long long n = ok ? nb + (long long)nnx * r + plane * j : 0;
+                const unsigned n = ok ? xu + (unsigned)nnx * (unsigned)(y - 1 + r) + plane * (unsigned)j : 0u;
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
                     R.row[r].r[c] = ok ? A.r[3 * n + c] : 0.f;
@@ -94,8 +95,9 @@ __global__ void __launch_bounds__(32 * kM3Warps) k_march3(const Mv3Args<float> A
             }
             const int ez = j - 1;
             const bool zok = elx && ez >= 0 && ez < nelz;
-            R.rho[0] = (zok && e0ok) ? A.escale[x + (long long)nelx * ((y - 1) + (long long)nely * ez)] : 0.f;
-            R.rho[1] = (zok && e1ok) ? A.escale[x + (long long)nelx * (y + (long long)nely * ez)] : 0.f;
+            const unsigned e1 = xu + (unsigned)nelx * ((unsigned)y + (unsigned)nely * (unsigned)ez);
+            R.rho[0] = (zok && e0ok) ? A.escale[e1 - (unsigned)nelx] : 0.f;
+            R.rho[1] = (zok && e1ok) ? A.escale[e1] : 0.f;
         };
         const int j0 = za - 1, j1 = zb;   // planes walked (inclusive)
         M3Plane buf[D];
@@ -185,7 +187,7 @@ __global__ void __launch_bounds__(32 * kM3Warps) k_march3(const Mv3Args<float> A
                         cO[c] = oU + (lane > 0 ? tU : 0.f);
                     }
                     if (j > za && own) {   // node (x, y, j - 1) is complete
-                        const long long n = nb + nnx + plane * (j - 1);
+                        const unsigned n = xu + (unsigned)nnx * (unsigned)y + plane * (unsigned)(j - 1);
 #pragma unroll
                         for (int c = 0; c < 3; ++c) {
                             pnew[3 * n + c] = pl1[c];
