@@ -534,8 +534,9 @@ __global__ void __launch_bounds__(256) k_mv3_finalize(const Mv3Args<T> A, const 
 // PCG update for the 3D operator: fixed rows q = meandiag p (= 0), then
 // x += alpha p, r -= alpha q, r.z and r.r partials.  q already holds K p: the
 // side partials of the tile-boundary nodes were added by k_side_gather3.  The FP32
-// dof arrays are streamed as float4 (4 dofs per thread and step).
-template <typename T>
+// dof arrays are streamed as float4 (4 dofs per thread and step), G groups per thread
+// and round with every load of the round issued before its first store.
+template <typename T, int G = 2>
 __global__ void __launch_bounds__(256) k_pcg_update3(const Mv3Args<T> A, T* __restrict__ x, T* __restrict__ r,
                                                      T meandiag, const LoopCond cond) {
     PcgState* st = A.st;
@@ -556,7 +557,6 @@ __global__ void __launch_bounds__(256) k_pcg_update3(const Mv3Args<T> A, T* __re
         const float4* __restrict__ p4 = reinterpret_cast<const float4*>(p);
         float4* __restrict__ x4 = reinterpret_cast<float4*>(x);
         float4* __restrict__ r4 = reinterpret_cast<float4*>(r);
-        // two float4 groups per thread and round, every load issued before the first store
         const unsigned stride = gridDim.x * blockDim.x;
         auto group = [&](unsigned g, const float4& qv, const float4& pv, const float4& xv, const float4& rv,
                          unsigned m0, unsigned m1, float d0, float d1, unsigned c0) {
@@ -589,20 +589,30 @@ __global__ void __launch_bounds__(256) k_pcg_update3(const Mv3Args<T> A, T* __re
             nb = n0 + 1 < nnodes ? n0 + 1 : n0;
         };
         unsigned g = blockIdx.x * blockDim.x + threadIdx.x;
-        for (; g + stride < nv; g += 2 * stride) {
-            const unsigned h2 = g + stride;
-            unsigned na, nab, ca, nc, ncb, cc2;
-            node_of(g, na, nab, ca);
-            node_of(h2, nc, ncb, cc2);
-            const float4 qa = q4[g], pa = p4[g], xa = x4[g], ra = r4[g];
-            const float4 qb = q4[h2], pb = p4[h2], xb = x4[h2], rb = r4[h2];
-            const unsigned ma0 = A.fixmask[na], ma1 = A.fixmask[nab], mb0 = A.fixmask[nc], mb1 = A.fixmask[ncb];
-            const float da0 = (float)A.dinv[na], da1 = (float)A.dinv[nab], db0 = (float)A.dinv[nc],
-                        db1 = (float)A.dinv[ncb];
-            group(g, qa, pa, xa, ra, ma0, ma1, da0, da1, ca);
-            group(h2, qb, pb, xb, rb, mb0, mb1, db0, db1, cc2);
+        for (; g + (G - 1) * stride < nv; g += G * stride) {   // G groups per round, all loads first
+            float4 qv[G], pv[G], xv[G], rv[G];
+            unsigned n0[G], n1[G], c0[G], m0[G], m1[G];
+            float d0[G], d1[G];
+#pragma unroll
+            for (int k = 0; k < G; ++k) {
+                const unsigned gk = g + k * stride;
+                node_of(gk, n0[k], n1[k], c0[k]);
+                qv[k] = q4[gk];
+                pv[k] = p4[gk];
+                xv[k] = x4[gk];
+                rv[k] = r4[gk];
+            }
+#pragma unroll
+            for (int k = 0; k < G; ++k) {
+                m0[k] = A.fixmask[n0[k]];
+                m1[k] = A.fixmask[n1[k]];
+                d0[k] = (float)A.dinv[n0[k]];
+                d1[k] = (float)A.dinv[n1[k]];
+            }
+#pragma unroll
+            for (int k = 0; k < G; ++k) group(g + k * stride, qv[k], pv[k], xv[k], rv[k], m0[k], m1[k], d0[k], d1[k], c0[k]);
         }
-        if (g < nv) {
+        for (; g < nv; g += stride) {
             unsigned na, nab, ca;
             node_of(g, na, nab, ca);
             group(g, q4[g], p4[g], x4[g], r4[g], A.fixmask[na], A.fixmask[nab], (float)A.dinv[na],
