@@ -647,7 +647,9 @@ __global__ void __launch_bounds__(32 * kMarchWarps) bk_march(BArgs A) {
         const bool elok = x >= 0 && x < nelx && lane < 31;
         const bool own = colok && lane >= 1 && lane <= 30;
         const bool fixed = (x == 0);
-        const long long nb = P.noff + x, eb = P.eoff + x;
+        // 32-bit node / cell indices (the batch holds fewer than 2^30 nodes); used only where
+        // the node or cell exists (x >= 0)
+        const unsigned nb = (unsigned)P.noff + (unsigned)x, eb = (unsigned)P.eoff + (unsigned)x;
         // per-item scalars and row loader
         T beta = T(0), sc = T(0);
         int odd = 0, mode = 0;
@@ -660,9 +662,9 @@ __global__ void __launch_bounds__(32 * kMarchWarps) bk_march(BArgs A) {
         }
         auto load = [&](int j, Row& R) {
             const bool rok = colok && j >= 0 && j < nny;
-            const long long n = nb + (long long)nnx * j;
+            const unsigned n = nb + (unsigned)nnx * (unsigned)j;
             const bool eok = elok && j >= 1 && j - 1 < nely;
-            const long long e = eb + (long long)nelx * (j - 1);
+            const unsigned e = eb + (unsigned)nelx * (unsigned)(j - 1);
             if constexpr (MODE == MV_PCG) {
                 const float2* pold = reinterpret_cast<const float2*>(odd ? A.P0 : A.P1);
                 R.r = rok ? reinterpret_cast<const float2*>(A.r32)[n] : make_float2(0.f, 0.f);
@@ -709,7 +711,7 @@ __global__ void __launch_bounds__(32 * kMarchWarps) bk_march(BArgs A) {
                     const T t3y = __shfl_up_sync(0xffffffffu, y[1][3], 1);
                     if (j > b0 && own) {   // node row j - 1 is complete
                         const T qx = carry.x + y[0][0] + t1x, qy = carry.y + y[1][0] + t1y;
-                        const long long n = nb + (long long)nnx * (j - 1);
+                        const unsigned n = nb + (unsigned)nnx * (unsigned)(j - 1);
                         if constexpr (MODE == MV_PCG) {
                             const float2 qv = fixed ? make_float2(0.f, 0.f) : make_float2(qx, qy);
                             reinterpret_cast<float2*>(odd ? A.P1 : A.P0)[n] = plo;
@@ -1369,6 +1371,10 @@ int tog_batch_create(int32_t nprob, const int32_t* nelx, const int32_t* nely, co
     }
     b->nnodes = noff;
     b->ncells = eoff;
+    if (noff >= (1LL << 30)) {   // the operator kernels index nodes and dofs in 32 bits
+        delete b;
+        return bfail(TOG_ERR_ARG, "tog_batch_create: the batch needs fewer than 2^30 nodes in all");
+    }
     const long long max_tiles = build_tiles(b, 8);   // the lowest band gives the most items
     build_tiles(b, b->LY);
     if (max_tiles > (1LL << 30)) {
