@@ -305,6 +305,9 @@ int tog_nn_param_count(const tog_nn* nn, int64_t* count);
 int tog_nn_get_params(tog_nn* nn, float* params);
 /* Also resets the optimiser state. */
 int tog_nn_set_params(tog_nn* nn, const float* params);
+/* Runs the network and synchronises its stream.  The convolutions run on the tcgen05 tensor
+ * cores with bounded waits: a wait that gives up makes this and every later tog_nn_forward /
+ * tog_nn_gradients / tog_nn_train_step (with a loss) call of the network return TOG_ERR_CUDA. */
 int tog_nn_forward(tog_nn* nn, const float* in_dev, float* out_dev);
 /* Mean squared error against target_dev and its gradient w.r.t. every parameter (host
  * vector of tog_nn_param_count floats; may be NULL); no update. */

@@ -527,7 +527,7 @@ struct tog_nn {
     float *gy = nullptr, *g0 = nullptr, *g0b = nullptr, *gu0 = nullptr, *g1 = nullptr, *g1b = nullptr, *gu1 = nullptr;
     float *g2 = nullptr, *g2b = nullptr, *gu2 = nullptr, *g3 = nullptr;
     double* d_loss = nullptr;
-    int* d_err = nullptr;           // set by a tensor-core kernel whose mbarrier wait timed out
+    int* d_err = nullptr;           // set by a tensor-core kernel whose mbarrier wait timed out (sticky)
     std::vector<void*> allocs;
     cudaStream_t stream = nullptr;
     int steps = 0;
