@@ -104,7 +104,7 @@ struct tog_handle {
     size_t npartials = 0;
     unsigned* d_cnt = nullptr;    // misc counters
     double* d_scalar = nullptr;   // misc results
-    PcgState* h_st = nullptr;     // pinned
+    PcgState* h_st = nullptr;     // pinned, two states (the FP32-IR segment reads both at once)
     OcState* h_oc = nullptr;
     double* h_scalar = nullptr;
     // filter
@@ -492,24 +492,43 @@ int sync_state(tog_handle* h, const PcgState* d_st) {
     return TOG_OK;
 }
 
-// Run the PCG iterations of the current state to done: one graph launch, one host
-// synchronisation.
+// Launch the PCG iterations of the current state (to done) as one graph launch, without
+// a host synchronisation.  A state that is already done runs no iteration: the graph's
+// condition kernel sees it.
+template <typename T>
+int launch_pcg_loop(tog_handle* h, bool energy = false) {
+    cudaGraphExec_t* g = std::is_same<T, double>::value ? (energy ? &h->g_pcg64e : &h->g_pcg64) : &h->g_pcg32;
+    if (!*g) TOG_TRY(build_pcg_graph<T>(h, g, energy));
+    TOG_CUDA(cudaGraphLaunch(*g, h->stream));
+    return TOG_OK;
+}
+
+// Kernels of one launch_pcg_loop that took the state from iteration it0 to it1: the
+// condition kernel and every pass of the body (the last one may end early: its remaining
+// kernels find the state done and return; one more pass when an EnergyCriteria check
+// ended the loop after the body's last update).
+template <typename T>
+void count_pcg_loop(tog_handle* h, int it0, int it1, bool energy = false) {
+    if (it1 <= it0 && !energy) {
+        TOG_LAUNCHED(1);
+        return;
+    }
+    const long long passes = (it1 - it0 + h->pcg_unroll - 1) / h->pcg_unroll + (energy ? 1 : 0);
+    TOG_LAUNCHED(1 + std::max(1LL, passes) * h->pcg_unroll *
+                         (std::is_same<T, double>::value ? h->graph_nodes64 : h->graph_nodes32));
+}
+
+// Run the PCG iterations of the current state to done: one graph launch and one host
+// synchronisation (plus one before, for the starting iteration count).
 template <typename T>
 int run_pcg(tog_handle* h, bool energy = false) {
-    cudaGraphExec_t* g = std::is_same<T, double>::value ? (energy ? &h->g_pcg64e : &h->g_pcg64) : &h->g_pcg32;
     PcgState* d_st = std::is_same<T, double>::value ? h->d_st64 : h->d_st32;
-    if (!*g) TOG_TRY(build_pcg_graph<T>(h, g, energy));
     TOG_TRY(sync_state(h, d_st));
     const int it0 = h->h_st->it;
     if (h->h_st->done) return TOG_OK;
-    TOG_CUDA(cudaGraphLaunch(*g, h->stream));
+    TOG_TRY(launch_pcg_loop<T>(h, energy));
     TOG_TRY(sync_state(h, d_st));
-    // launches of this segment: the condition kernel and every pass of the body (the last
-    // one may end early: its remaining kernels find the state done and return; one more
-    // pass when an EnergyCriteria check ended the loop after the body's last update)
-    const long long passes = (h->h_st->it - it0 + h->pcg_unroll - 1) / h->pcg_unroll + (energy ? 1 : 0);
-    TOG_LAUNCHED(1 + std::max(1LL, passes) * h->pcg_unroll *
-                         (std::is_same<T, double>::value ? h->graph_nodes64 : h->graph_nodes32));
+    count_pcg_loop<T>(h, it0, h->h_st->it, energy);
     return TOG_OK;
 }
 
@@ -595,14 +614,24 @@ int solve_fp32_ir(tog_handle* h, double rtol, double abstol, int maxit, int warm
         TOG_CUDA(cudaGetLastError());
         double best = res;
         int since_best = 0;
+        int it0 = 0;   // FP32 iteration count at the start of the segment
         for (;;) {
-            TOG_TRY(run_pcg<float>(h));
-            const PcgState s32 = *h->h_st;
-            inner = s32.it;
+            // one segment: the FP32 PCG loop, the fold into u and the FP64 true residual,
+            // then one host synchronisation for both states
+            TOG_TRY(launch_pcg_loop<float>(h));
             k_ir_correct<<<nb, kEwThreads, 0, h->stream>>>(h->d_u, h->d_x32, nd, s);
             TOG_LAUNCHED(1);
+            launch_matvec<double, MV_RESID>(h, h->stream, h->d_u, h->d_r64, h->d_f);
+            TOG_CUDA(cudaGetLastError());
+            TOG_CUDA(cudaMemcpyAsync(h->h_st, h->d_st32, sizeof(PcgState), cudaMemcpyDeviceToHost, h->stream));
+            TOG_CUDA(cudaMemcpyAsync(h->h_st + 1, h->d_st64, sizeof(PcgState), cudaMemcpyDeviceToHost, h->stream));
+            TOG_CUDA(cudaStreamSynchronize(h->stream));
+            const PcgState s32 = h->h_st[0];
+            count_pcg_loop<float>(h, it0, s32.it);
+            inner = s32.it;
+            it0 = s32.it;
+            res = std::sqrt(h->h_st[1].rr);
             ++updates;
-            TOG_TRY(resid(&res));
             if (!std::isfinite(res)) {
                 status = TOG_BREAKDOWN;
                 break;
@@ -629,6 +658,7 @@ int solve_fp32_ir(tog_handle* h, double rtol, double abstol, int maxit, int warm
                 launch_pcg_init<float>(h, h->stream, 1, 0.0, tol / res, -1.0, maxit - inner,
                                        h->ru_delta * h->ru_delta);
                 s = res;
+                it0 = 0;
                 continue;
             }
             const double t2 = (tol / res) * (tol / res);
@@ -1333,7 +1363,7 @@ int tog_create(const tog_problem_desc* desc, tog_handle** out) {
         auto C = [&](cudaError_t x) {
             if (ee == cudaSuccess) ee = x;
         };
-        C(cudaHostAlloc((void**)&h->h_st, sizeof(PcgState), cudaHostAllocDefault));
+        C(cudaHostAlloc((void**)&h->h_st, 2 * sizeof(PcgState), cudaHostAllocDefault));   // FP32, FP64 segment states
         C(cudaHostAlloc((void**)&h->h_oc, sizeof(OcState), cudaHostAllocDefault));
         C(cudaHostAlloc((void**)&h->h_scalar, 8 * sizeof(double), cudaHostAllocDefault));
         C(cudaMemcpyAsync(h->d_int2ref, h->node_dofs.data(), N * sizeof(int), cudaMemcpyHostToDevice, h->own));
